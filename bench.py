@@ -1,0 +1,373 @@
+"""Benchmark of the batch RMQ hot path on one GB300 (replicas on N GPUs).
+
+Workload (the reference's headline, README.md:6, csv-to-plot/perf-*-ALG5.csv):
+plain RMQ over n = 1e8 float32 values uniform in [0,1) (seed 1321) with
+q = 2^26 inclusive (l, r) queries, values and leftmost indices both returned.
+The headline step is one rmq_query over the uniform-length queries (lr=-1);
+the other length modes of the same configuration (lr=-2, lr=-3, fixed
+len 2^10) are timed the same way and reported under "modes". The block size
+of each mode is the fastest of a sweep over 2^10..2^16.
+
+value      -- RMQ/s of the device-resident step (inputs already in HBM),
+              timed with CUDA events on the launching stream.
+e2e        -- the same step through the C ABI with host buffers: pinned
+              queries copied in, results (values + indices) copied out,
+              all inside the timed region.
+roofline   -- algorithmic HBM bytes per launch (query read + result write +
+              one 32-byte sector per pre/suf lookup, 32 bytes per sector a
+              block scan touches) / kernel time, against the measured copy
+              bandwidth.
+cpu_baseline -- the CPU oracle's restatement of the reference's
+              block-decomposition path on this host's cores, on a bounded
+              sample of the same queries.
+
+`--impl reference` times that CPU path alone (rank 0) and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_ELEMS = 10**8
+N_QUERIES = 1 << 26
+SEED = 1321
+MODES = [("lr=-1", -1), ("lr=-2", -2), ("lr=-3", -3), ("len=2^10", 1024)]
+BS_SWEEP = [1 << 10, 1 << 12, 1 << 14, 1 << 16]
+PUBLISHED_LR1 = 3.52e8  # RTXRMQ alg 5, RTX 6000 Ada (csv-to-plot/perf-RTX6000ADA-ALG5.csv:1586-1601)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_ELEMS)
+    ap.add_argument("--q", type=int, default=N_QUERIES)
+    ap.add_argument("--modes", default="all", help="comma list of lr values or 'all'")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- helpers
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons, n_load = [], None, set(), 0
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                clk, cmax, util = float(f[1]), float(f[2]), float(f[4])
+            except ValueError:
+                continue
+            mx = cmax
+            if util >= 50:
+                n_load += 1
+                sm.append(clk)
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(self.lines), "samples_under_load": n_load}
+
+
+def algorithmic_bytes(Q: np.ndarray, n: int, bs: int, out_bytes: int) -> tuple[float, dict]:
+    """HBM bytes the query kernel must move for this query set, following
+    the kernel's own decision per query (see query.cu)."""
+    l = Q[:, 0].astype(np.int64)
+    r = Q[:, 1].astype(np.int64)
+    lB, rB = l // bs, r // bs
+    cross = lB != rB
+    bstart = lB * bs
+    bend = np.minimum(bstart + bs, n) - 1
+    edge = (~cross) & ((l == bstart) | (r == bend))
+    scan = (~cross) & ~edge
+    sectors = (r * 4) // 32 - (l * 4) // 32 + 1
+    per_q = 8 + out_bytes
+    total = (per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge.sum() +
+             32.0 * sectors[scan].sum())
+    return float(total), {"cross_block": float(cross.mean()), "edge": float(edge.mean()),
+                          "scan": float(scan.mean()),
+                          "mean_scan_sectors": float(sectors[scan].mean()) if scan.any() else 0.0}
+
+
+def time_steps(fn, steps, warmup, stream, barrier):
+    import torch
+    for _ in range(warmup):
+        fn()
+    barrier()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        fn()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    return t0.elapsed_time(t1) / steps  # ms per step
+
+
+# ---------------------------------------------------------------- CPU side
+
+def cpu_sample_rate(A, Q, bs, target_s=12.0, nt=0):
+    """Oracle port of RTX_blocks on the host cores over a bounded query sample."""
+    import oracle
+    nt = nt or os.cpu_count() or 1
+    t = time.perf_counter()
+    ob = oracle.Blocks(A, bs, nt)
+    build_s = time.perf_counter() - t
+    rng = np.random.default_rng(5)
+    probe = Q[rng.integers(0, len(Q), 2048)]
+    t = time.perf_counter()
+    ob.query(probe, nt)
+    per = (time.perf_counter() - t) / len(probe)
+    m = int(min(len(Q), max(4096, target_s / max(per, 1e-9))))
+    sample = Q[rng.integers(0, len(Q), m)]
+    t = time.perf_counter()
+    ob.query(sample, nt)
+    dt = time.perf_counter() - t
+    ob.close()
+    return m / dt, {"cores": nt, "sample": f"{m} random queries of the step's query set "
+                    f"(n={len(A)}, bs={bs}), {dt:.1f} s", "construction_s": build_s}
+
+
+def cpu_bs(n):
+    # block size minimising bs + n/bs per query for the O(bs + nb) CPU path
+    return int(max(1, round(n ** 0.5)))
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import oracle
+    import rtxrmq_gb300 as R
+    oracle.build(with_ref=False)
+    nt = os.cpu_count() or 1
+    n, q = args.n, args.q
+    A = R.gen_values_uniform(n, SEED)
+    Q = R.gen_queries(q, n, -1, SEED + 1)
+    bs = cpu_bs(n)
+    ob = oracle.Blocks(A, bs, nt)
+    rng = np.random.default_rng(9)
+    probe = Q[rng.integers(0, q, 1024)]
+    t = time.perf_counter()
+    ob.query(probe, nt)
+    per = (time.perf_counter() - t) / len(probe)
+    m = int(max(1024, min(q, 1.5 / max(per, 1e-9))))  # ~1.5 s of work per step
+    for _ in range(args.warmup):
+        ob.query(Q[rng.integers(0, q, m)], nt)
+    times = []
+    for _ in range(args.steps):
+        s = Q[rng.integers(0, q, m)]
+        t = time.perf_counter()
+        ob.query(s, nt)
+        times.append(time.perf_counter() - t)
+    v = m * args.steps / sum(times)
+    line = {"metric": "RMQ/s n=1e8 q=2^26 lr=-1 (values+indices)", "value": v, "unit": "RMQ/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices",
+                       "n": n, "q": q, "lr": -1, "seed": SEED},
+            "cpu_baseline": {"value": v, "unit": "RMQ/s", "cores": nt, "kind": "port",
+                             "sample": f"{m} random queries per step from the 2^26-query set, "
+                                       f"oracle restatement of RTX_blocks (bs={bs}) on {nt} threads"},
+            "e2e": {"value": v, "unit": "RMQ/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    import rtxrmq_gb300 as R
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    n, q = args.n, args.q
+    hbm_peak, peak_kind = peaks()
+
+    A = R.gen_values_uniform(n, SEED)
+    dA = torch.from_numpy(A).to(dev)
+    modes = MODES if args.modes == "all" else [(f"lr={m}", int(m)) for m in args.modes.split(",")]
+    out_v = torch.empty(q, dtype=torch.float32, device=dev)
+    out_i = torch.empty(q, dtype=torch.int32, device=dev)
+
+    results = {}
+    headline = None
+    sampler = ClockSampler(local)
+    with sampler:
+        for name, lr in modes:
+            # replicas: each rank answers its own query set (seeded by rank)
+            Q = R.gen_queries(q, n, lr, SEED + 1 + 1000 * rank + (0 if lr == -1 else 17 * abs(lr)))
+            dQ = torch.from_numpy(Q).to(dev)
+            sweep = {}
+            best = None
+            for bs in BS_SWEEP:
+                ix = R.RMQIndex(dA, bs)
+                fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+                ms = time_steps(fn, 3, 1, stream, barrier)
+                sweep[bs] = q / (ms / 1e3)
+                if best is None or ms < best[1]:
+                    best = (bs, ms)
+                ix.close()
+            bs = best[0]
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            ix = R.RMQIndex(dA, bs)
+            torch.cuda.synchronize()
+            construction_ms = (time.perf_counter() - t) * 1e3
+            fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+            ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
+            if world > 1:
+                tt = torch.tensor([ms], device=dev)
+                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+                ms = float(tt.item())
+            alg_bytes, mix = algorithmic_bytes(Q, n, bs, 8)
+            res = {"value": world * q / (ms / 1e3), "ms_per_step": ms, "bs": bs,
+                   "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
+                   "construction_ms": construction_ms, "mix": mix,
+                   "alg_bytes_per_step": alg_bytes,
+                   "achieved_gbs": alg_bytes / (ms / 1e3) / 1e9,
+                   "info": ix.info()}
+            if lr == -1:
+                # end to end through the C ABI with host buffers
+                hQ = torch.from_numpy(Q).pin_memory()
+                hV = torch.empty(q, dtype=torch.float32).pin_memory()
+                hI = torch.empty(q, dtype=torch.int32).pin_memory()
+                dQ2 = torch.empty_like(dQ)
+
+                def e2e():
+                    dQ2.copy_(hQ, non_blocking=True)
+                    ix.query(dQ2, out_val=out_v, out_idx=out_i)
+                    hV.copy_(out_v, non_blocking=True)
+                    hI.copy_(out_i, non_blocking=True)
+
+                e2e_ms = time_steps(e2e, args.steps, args.warmup, stream, barrier)
+                if world > 1:
+                    tt = torch.tensor([e2e_ms], device=dev)
+                    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+                    e2e_ms = float(tt.item())
+                torch.cuda.synchronize()
+                ok = (np.array_equal(hI[:4096].numpy(), out_i[:4096].cpu().numpy()))
+                res["e2e"] = {"value": world * q / (e2e_ms / 1e3), "unit": "RMQ/s",
+                              "h2d_bytes_per_step": int(Q.nbytes),
+                              "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
+                              "ms_per_step": e2e_ms, "copy_check": bool(ok)}
+                headline = (name, lr, Q, bs)
+                del hQ, hV, hI, dQ2
+            ix.close()
+            results[name] = res
+            del dQ
+    clocks = sampler.summary()
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    name, lr, Q, bs = headline if headline else (modes[0][0], modes[0][1], None, None)
+    h = results[name]
+    achieved = h["achieved_gbs"]
+    line = {
+        "metric": "RMQ/s n=1e8 q=2^26 lr=-1 (values+indices)",
+        "value": h["value"], "unit": "RMQ/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": h["value"] / PUBLISHED_LR1,
+        "vs_baseline_ref": "RTXRMQ (alg 5) on RTX 6000 Ada, 3.52e8 RMQ/s, n=1e8 q=2^26 lr=-1",
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices",
+                   "n": n, "q": q, "lr": lr, "bs": bs, "seed": SEED,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "no flush: per-step working set (2.9 GB: values, pre/suf, queries, "
+                         "outputs) is larger than L2"},
+        "e2e": h.get("e2e"),
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_kind": f"{peak_kind} copy bandwidth",
+                     "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
+        "clocks": clocks,
+        "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
+    }
+    if not args.no_cpu and world == 1:
+        cbs = cpu_bs(n)
+        v, meta = cpu_sample_rate(A, Q, cbs)
+        line["cpu_baseline"] = {"value": v, "unit": "RMQ/s", "cores": meta["cores"], "kind": "port",
+                                "sample": meta["sample"]}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

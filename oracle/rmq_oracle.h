@@ -1,0 +1,29 @@
+/*
+ * rmq_oracle.h -- CPU oracle (test infrastructure only; see rmq_oracle.c).
+ */
+#ifndef RMQ_ORACLE_H
+#define RMQ_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* BASE: src/cpu_methods.h:6-77 restated (leftmost, strict `<`). */
+int oracle_base_val(const float *A, int64_t n, const int32_t *Q, int64_t q, float *out, int nt);
+int oracle_base_idx(const float *A, int64_t n, const int32_t *Q, int64_t q, int32_t *out, int nt);
+
+/* RTX_blocks decomposition restated (src/rtx_kernels.cu:85-180, src/rtx.h:3-22). */
+typedef struct oracle_blocks oracle_blocks_t;
+oracle_blocks_t *oracle_blocks_build(const float *A, int64_t n, int64_t bs, int nt);
+int oracle_blocks_query(const oracle_blocks_t *o, const int32_t *Q, int64_t q, float *val,
+                        int32_t *idx, int nt);
+void oracle_blocks_free(oracle_blocks_t *o);
+
+int oracle_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

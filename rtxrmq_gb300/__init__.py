@@ -1,0 +1,214 @@
+"""rtxrmq_gb300 -- GB300-native batch range-minimum queries (RMQ).
+
+Host-side mirror of the reference's interface for its hot path
+(``rtx_rmq<T>(alg, n, bs, q, darray, dquery, args)``, src/rtx.h:24-177, with
+alg 5 returning values and alg 105 returning indices; ``gpu_rmq_basic`` /
+``gpu_rmq_basic_idx``, src/cuda_methods.cuh:69-169) over the C ABI of
+include/rmq.h. Device buffers are torch CUDA tensors (used only as device
+memory and streams); every computation runs in librmq.so.
+
+Semantics for an inclusive query (l, r): value = min A[l..r] (the exact bits
+of A[idx]) and idx = the leftmost position holding it, as the reference's
+BASE oracles (src/cpu_methods.h:42-53).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Tuple
+
+import numpy as np
+
+from ._native import LIB_PATH, RMQError, check, load, rmq_info_t
+
+__all__ = [
+    "RMQIndex", "RMQError", "rtx_rmq", "gpu_rmq_basic", "gpu_rmq_basic_idx", "bs_from_nb",
+    "gen_values_uniform", "gen_values_normal", "gen_values_int", "gen_queries",
+    "gen_queries_lognormal", "ALG_GPU_BASE", "ALG_GPU_RTX_BLOCKS", "ALG_GPU_BASE_IDX",
+    "ALG_GPU_RTX_BLOCKS_IDX", "DEFAULT_BS", "LIB_PATH", "load",
+]
+
+# algorithm ids of src/main.cu:17-32 that this engine serves
+ALG_GPU_BASE = 2
+ALG_GPU_RTX_BLOCKS = 5
+ALG_GPU_BASE_IDX = 102
+ALG_GPU_RTX_BLOCKS_IDX = 105
+DEFAULT_BS = 1 << 15  # src/tools.h:96
+
+
+def _stream_handle(stream) -> Optional[int]:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def _dptr(t) -> Optional[int]:
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return t.data_ptr()
+
+
+def _check_queries(queries):
+    import torch
+    if queries.dtype != torch.int32:
+        raise TypeError("queries must be int32 (l, r) pairs")
+    if queries.dim() != 2 or queries.shape[1] != 2:
+        raise ValueError("queries must have shape [q, 2]")
+    return queries.shape[0]
+
+
+class RMQIndex:
+    """Block-decomposition index over a float32 CUDA tensor.
+
+    Construction is the GPU replacement of RTX_blocks' geometry + BVH build
+    (src/rtx.h:39-99); ``query`` replaces the timed optixLaunch
+    (src/rtx.h:150-154). ``values`` must stay alive and unchanged while the
+    index is used (the index refers to it, it does not copy it).
+    """
+
+    def __init__(self, values, bs: int = 0, stream=None):
+        import torch
+        if values.dtype != torch.float32 or values.dim() != 1:
+            raise TypeError("values must be a 1-D float32 CUDA tensor")
+        lib = load()
+        self._values = values
+        self._h = C.c_void_p()
+        check(lib.rmq_build(_dptr(values), values.numel(), int(bs), _stream_handle(stream),
+                            C.byref(self._h)))
+
+    def info(self) -> dict:
+        inf = rmq_info_t()
+        check(load().rmq_info(self._h, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in rmq_info_t._fields_}
+
+    def query(self, queries, *, values: bool = True, indices: bool = True, out_val=None,
+              out_idx=None, stream=None) -> Tuple:
+        """Answer int32 [q, 2] queries; returns (val, idx), either may be None."""
+        import torch
+        q = _check_queries(queries)
+        dev = queries.device
+        if values and out_val is None:
+            out_val = torch.empty(q, dtype=torch.float32, device=dev)
+        if indices and out_idx is None:
+            out_idx = torch.empty(q, dtype=torch.int32, device=dev)
+        if not values:
+            out_val = None
+        if not indices:
+            out_idx = None
+        check(load().rmq_query(self._h, _dptr(queries), q, _dptr(out_val), _dptr(out_idx),
+                               _stream_handle(stream)))
+        return out_val, out_idx
+
+    def invalid_count(self, stream=None) -> int:
+        v = C.c_int64()
+        check(load().rmq_invalid_count(self._h, _stream_handle(stream), C.byref(v)))
+        return v.value
+
+    @property
+    def handle(self) -> int:
+        return self._h.value or 0
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            check(load().rmq_free(self._h))
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def bs_from_nb(n: int, nb: int) -> int:
+    """--nb semantics of src/tools.h:129-132: bs = n // min(n, nb)."""
+    bs = C.c_int64()
+    check(load().rmq_bs_from_nb(n, nb, C.byref(bs)))
+    return bs.value
+
+
+def rtx_rmq(alg: int, n: int, bs: int, q: int, darray, dquery, reps: int = 1) -> np.ndarray:
+    """Mirror of ``rtx_rmq<T>`` (src/rtx.h:24-177) for alg 5 / 105.
+
+    Builds the index over ``darray[:n]`` with block size ``bs``, answers the
+    first ``q`` queries of ``dquery`` ``reps`` times, and returns a host array:
+    float32 values for alg 5, int32 indices for alg 105.
+    """
+    import torch
+    if alg not in (ALG_GPU_RTX_BLOCKS, ALG_GPU_RTX_BLOCKS_IDX):
+        raise RMQError(-5, f"alg {alg} is not served by rtx_rmq (use 5 or 105)")
+    want_idx = alg >= 100
+    with RMQIndex(darray[:n], bs) as ix:
+        out = None
+        for _ in range(max(1, reps)):
+            v, i = ix.query(dquery[:q], values=not want_idx, indices=want_idx)
+            out = i if want_idx else v
+        torch.cuda.current_stream().synchronize()
+        return out.cpu().numpy()
+
+
+def _gpu_base(n: int, q: int, darray, dquery, want_idx: bool) -> np.ndarray:
+    import torch
+    _check_queries(dquery[:q])
+    dev = dquery.device
+    val = None if want_idx else torch.empty(q, dtype=torch.float32, device=dev)
+    idx = torch.empty(q, dtype=torch.int32, device=dev) if want_idx else None
+    check(load().rmq_query_scan(_dptr(darray), n, _dptr(dquery[:q]), q, _dptr(val), _dptr(idx),
+                                _stream_handle(None)))
+    torch.cuda.current_stream().synchronize()
+    return (idx if want_idx else val).cpu().numpy()
+
+
+def gpu_rmq_basic(n: int, q: int, darray, dquery) -> np.ndarray:
+    """Mirror of gpu_rmq_basic (alg 2, src/cuda_methods.cuh:69-101): values."""
+    return _gpu_base(n, q, darray, dquery, False)
+
+
+def gpu_rmq_basic_idx(n: int, q: int, darray, dquery) -> np.ndarray:
+    """Mirror of gpu_rmq_basic_idx (alg 102, src/cuda_methods.cuh:103-135): indices."""
+    return _gpu_base(n, q, darray, dquery, True)
+
+
+# ---- synthetic inputs (host) ----
+
+def gen_values_uniform(n: int, seed: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.float32)
+    check(load().rmq_gen_values_uniform(out.ctypes.data, n, seed & (2**64 - 1)))
+    return out
+
+
+def gen_values_normal(n: int, seed: int, mean: float = 0.0, std: float = 1.0) -> np.ndarray:
+    out = np.empty(n, dtype=np.float32)
+    check(load().rmq_gen_values_normal(out.ctypes.data, n, mean, std, seed & (2**64 - 1)))
+    return out
+
+
+def gen_values_int(n: int, value_range: int, seed: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.float32)
+    check(load().rmq_gen_values_int(out.ctypes.data, n, value_range, seed & (2**64 - 1)))
+    return out
+
+
+def gen_queries(q: int, n: int, lr: int, seed: int) -> np.ndarray:
+    """int32 [q, 2] queries with the reference's length modes (lr > 0, -1 .. -5)."""
+    out = np.empty((q, 2), dtype=np.int32)
+    check(load().rmq_gen_queries(out.ctypes.data, q, n, lr, seed & (2**64 - 1)))
+    return out
+
+
+def gen_queries_lognormal(q: int, n: int, mu: float, sigma: float, seed: int) -> np.ndarray:
+    out = np.empty((q, 2), dtype=np.int32)
+    check(load().rmq_gen_queries_lognormal(out.ctypes.data, q, n, mu, sigma, seed & (2**64 - 1)))
+    return out

@@ -1,0 +1,54 @@
+// engine.h -- internal interface between the C ABI (api.cu) and the kernel
+// translation units. Nothing here is exported.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace rmq {
+
+// Records a message for rmq_last_error_string() and returns `code`.
+int set_error(int code, const char *fmt, ...);
+// Converts a CUDA error into RMQ_ECUDA with the call site in the message.
+int cuda_fail(cudaError_t err, const char *what);
+
+// Device properties the launchers need, cached per device.
+struct DeviceInfo {
+    int device;
+    int sms;
+    size_t l2_bytes;
+};
+int device_info(DeviceInfo *out);
+
+// ---- plain index (build.cu) ----
+struct BuildPlan {
+    const float *A;
+    uint32_t n;
+    uint32_t bs;
+    uint32_t nb;
+    uint32_t levels;
+    bool aligned;
+    Entry *pre;   // [n]
+    Entry *suf;   // [n]
+    Entry *st;    // [levels * nb], level 0 = block minima
+};
+uint32_t st_levels(uint32_t nb);
+cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s);
+
+// ---- queries (query.cu) ----
+struct QueryArgs {
+    const int2 *Q;
+    int64_t q;
+    float *val;
+    int32_t *idx;
+    unsigned long long *invalid;  // device counter, may be null
+};
+cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,
+                         cudaStream_t s);
+cudaError_t launch_query_scan(const float *A, uint32_t n, const QueryArgs &a,
+                              const DeviceInfo &dev, cudaStream_t s);
+
+}  // namespace rmq

@@ -1,0 +1,225 @@
+"""GPU parity of the block-decomposition engine (alg 5 / 105) through the C
+ABI, against the CPU oracle (restatement of the reference's BASE, pinned to
+the reference's own outputs by tests/test_oracle_golden.py).
+
+Bar: bit-exact values (the bits of A[idx]) and exact leftmost indices.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted((Path(__file__).parent / "golden").glob("*.npz"))
+
+
+def bits(x):
+    return np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+
+
+def run_index(cuda, A, Q, bs, values=True, indices=True):
+    import torch
+
+    import rtxrmq_gb300 as R
+    dA = torch.from_numpy(np.ascontiguousarray(A, dtype=np.float32)).to(cuda)
+    dQ = torch.from_numpy(np.ascontiguousarray(Q, dtype=np.int32)).to(cuda)
+    with R.RMQIndex(dA, bs) as ix:
+        v, i = ix.query(dQ, values=values, indices=indices)
+        torch.cuda.synchronize()
+        return (None if v is None else v.cpu().numpy()), (None if i is None else i.cpu().numpy())
+
+
+def assert_matches(A, Q, v, i, ev, ei):
+    if i is not None:
+        bad = np.nonzero(i != ei)[0]
+        assert bad.size == 0, (f"{bad.size} index mismatches; first q={bad[0]} "
+                               f"(l,r)={tuple(Q[bad[0]])} got {i[bad[0]]} want {ei[bad[0]]}")
+    if v is not None:
+        np.testing.assert_array_equal(bits(v), bits(ev))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: p.stem)
+@pytest.mark.parametrize("bs", [1, 2, 5, 32, 100, 1000, 4096, 1 << 15])
+def test_golden_vectors(cuda, native, path, bs):
+    """Engine output equals the reference's BASE outputs stored in the fixtures."""
+    g = np.load(path)
+    v, i = run_index(cuda, g["A"], g["Q"], bs)
+    assert_matches(g["A"], g["Q"], v, i, g["base_val"], g["base_idx"])
+
+
+def all_pairs(n):
+    l, r = np.triu_indices(n)
+    return np.stack([l, r], axis=1).astype(np.int32)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 31, 32, 33, 127, 300])
+def test_exhaustive_small(cuda, native, oracle_lib, n):
+    """Every (l, r) of small tie-heavy arrays, across block sizes that put
+    block edges everywhere (bs = 1 .. n)."""
+    import rtxrmq_gb300 as R
+    A = R.gen_values_int(n, 4, n)
+    Q = all_pairs(n)
+    ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
+    for bs in sorted({1, 2, 3, 4, 7, 8, 16, 31, 32, 33, 64, 100, 128, n, max(1, n // 2)}):
+        if bs > n:
+            continue
+        v, i = run_index(cuda, A, Q, bs)
+        assert_matches(A, Q, v, i, ev, ei)
+
+
+@pytest.mark.parametrize("bs", [1 << 10, 1 << 12, 1 << 15, 0, 977])
+def test_config_small_range(cuda, native, oracle_lib, bs):
+    """n=1e6 uniform values (seed 1321), q=2^20 small-range (lr=-3) queries."""
+    import rtxrmq_gb300 as R
+    n, q = 10**6, 1 << 20
+    A = R.gen_values_uniform(n, 1321)
+    Q = R.gen_queries(q, n, -3, 1321)
+    v, i = run_index(cuda, A, Q, bs)
+    assert_matches(A, Q, v, i, oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q))
+
+
+@pytest.mark.parametrize("lr", [-1, -2, -3, 1, 32, 1024, 65536])
+@pytest.mark.parametrize("bs", [1 << 10, 1 << 13, 1 << 16, 12207])
+def test_length_modes_medium(cuda, native, oracle_lib, lr, bs):
+    """n=2^22: every length mode and block-size class; oracle = the CPU
+    restatement of RTX_blocks (exact, O(bs + nb) per query)."""
+    import rtxrmq_gb300 as R
+    n, q = 1 << 22, 1 << 16
+    A = R.gen_values_uniform(n, 11)
+    Q = R.gen_queries(q, n, lr, 100 + lr)
+    v, i = run_index(cuda, A, Q, bs)
+    ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
+    assert_matches(A, Q, v, i, ev, ei)
+
+
+@pytest.mark.parametrize("length", [1, 32, 1 << 10, 1 << 16, 1 << 20])
+def test_tie_heavy(cuda, native, oracle_lib, length):
+    """Integers in [0,256): most ranges hold many equal minima; leftmost."""
+    import rtxrmq_gb300 as R
+    n, q = 1 << 23, 1 << 15
+    A = R.gen_values_int(n, 256, 3)
+    Q = R.gen_queries(q, n, length, 7)
+    ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
+    for bs in (1 << 10, 1 << 16):
+        v, i = run_index(cuda, A, Q, bs)
+        assert_matches(A, Q, v, i, ev, ei)
+
+
+def test_special_values(cuda, native, oracle_lib):
+    """+-0 compare equal (leftmost wins, its own sign returned), +-inf,
+    subnormals, negatives."""
+    rng = np.random.default_rng(0)
+    n = 50_000
+    A = rng.standard_normal(n).astype(np.float32)
+    for val, cnt in ((0.0, 3000), (-0.0, 3000), (np.inf, 100), (-np.inf, 100), (1e-42, 100)):
+        A[rng.integers(0, n, cnt)] = val
+    import rtxrmq_gb300 as R
+    Q = np.concatenate([R.gen_queries(20000, n, L, L) for L in (1, 2, 9, 333, 4000)])
+    ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
+    for bs in (1, 64, 1024, 50_000):
+        v, i = run_index(cuda, A, Q, bs)
+        assert_matches(A, Q, v, i, ev, ei)
+    # only zeros: every answer is the leftmost zero with its own sign
+    Z = np.where(rng.random(4096) < 0.5, np.float32(0.0), np.float32(-0.0)).astype(np.float32)
+    Qz = all_pairs(200)
+    v, i = run_index(cuda, Z, Qz, 16)
+    np.testing.assert_array_equal(i, Qz[:, 0])
+    np.testing.assert_array_equal(bits(v), bits(Z[Qz[:, 0]]))
+
+
+def test_outputs_optional(cuda, native, oracle_lib):
+    import rtxrmq_gb300 as R
+    n = 10_000
+    A = R.gen_values_uniform(n, 4)
+    Q = R.gen_queries(5000, n, -1, 4)
+    v, i = run_index(cuda, A, Q, 100, values=True, indices=False)
+    assert i is None
+    np.testing.assert_array_equal(bits(v), bits(oracle_lib.base_val(A, Q)))
+    v, i = run_index(cuda, A, Q, 100, values=False, indices=True)
+    assert v is None
+    np.testing.assert_array_equal(i, oracle_lib.base_idx(A, Q))
+
+
+def test_unaligned_values(cuda, native, oracle_lib):
+    """A values pointer that is not 16-byte aligned takes the scalar-load path."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = 70_001
+    A = R.gen_values_int(n + 3, 50, 9)
+    Q = R.gen_queries(20000, n, -3, 2)
+    Q = np.concatenate([Q, R.gen_queries(5000, n, -1, 3)])
+    big = torch.from_numpy(A).to(cuda)
+    for off in (1, 2, 3):
+        dA = big[off:off + n]
+        dQ = torch.from_numpy(Q).to(cuda)
+        with R.RMQIndex(dA, 1000) as ix:
+            assert ix.info()["aligned"] == 0
+            v, i = ix.query(dQ)
+            torch.cuda.synchronize()
+        Ah = A[off:off + n]
+        np.testing.assert_array_equal(i.cpu().numpy(), oracle_lib.base_idx(Ah, Q))
+        np.testing.assert_array_equal(bits(v.cpu().numpy()), bits(oracle_lib.base_val(Ah, Q)))
+
+
+def test_invalid_queries(cuda, native):
+    """l > r, r >= n, l < 0: idx -1, NaN value, counted; valid ones unaffected."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = 1000
+    A = R.gen_values_uniform(n, 1)
+    Q = np.array([[0, 999], [5, 4], [0, 1000], [-1, 3], [10, 10], [999, 999], [2**31 - 1, 2**31 - 1]],
+                 dtype=np.int32)
+    dA = torch.from_numpy(A).to(cuda)
+    with R.RMQIndex(dA, 64) as ix:
+        v, i = ix.query(torch.from_numpy(Q).to(cuda))
+        assert ix.invalid_count() == 4
+        v, i = v.cpu().numpy(), i.cpu().numpy()
+    assert list(i) == [int(np.argmin(A)), -1, -1, -1, 10, 999, -1]
+    assert np.isnan(v[[1, 2, 3, 6]]).all()
+    assert v[0] == A.min()
+
+
+def test_gpu_base_matches_oracle(cuda, native, oracle_lib):
+    """alg 2 / 102 (GPU brute force) equals BASE, including on the fixtures."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    for path in GOLDEN:
+        g = np.load(path)
+        dA = torch.from_numpy(g["A"]).to(cuda)
+        dQ = torch.from_numpy(g["Q"]).to(cuda)
+        q = len(g["Q"])
+        np.testing.assert_array_equal(R.gpu_rmq_basic_idx(len(g["A"]), q, dA, dQ), g["base_idx"])
+        np.testing.assert_array_equal(bits(R.gpu_rmq_basic(len(g["A"]), q, dA, dQ)), bits(g["base_val"]))
+
+
+def test_rtx_rmq_mirror(cuda, native, oracle_lib):
+    """rtx_rmq(alg, n, bs, q, dA, dQ) mirrors src/rtx.h:24-177 for 5 / 105."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n, q = 50_000, 20_000
+    A = R.gen_values_uniform(n, 8)
+    Q = R.gen_queries(q, n, -2, 8)
+    dA, dQ = torch.from_numpy(A).to(cuda), torch.from_numpy(Q).to(cuda)
+    vals = R.rtx_rmq(5, n, R.bs_from_nb(n, 512), q, dA, dQ, reps=2)
+    idx = R.rtx_rmq(105, n, 1 << 10, q, dA, dQ)
+    assert vals.dtype == np.float32 and idx.dtype == np.int32
+    np.testing.assert_array_equal(bits(vals), bits(oracle_lib.base_val(A, Q)))
+    np.testing.assert_array_equal(idx, oracle_lib.base_idx(A, Q))
+    with pytest.raises(R.RMQError):
+        R.rtx_rmq(3, n, 1024, q, dA, dQ)
+
+
+def test_cli_check_passes(native):
+    """The CLI's --check (src/main.cu:140-167) passes for algs 5 and 105."""
+    import subprocess
+    cli = Path(__file__).resolve().parent.parent / "rtxrmq_gb300" / "_lib" / "rtxrmq"
+    for alg in ("5", "105", "2", "102"):
+        r = subprocess.run([str(cli), "200000", "100000", "-3", alg, "--bs", "1024", "--reps", "2",
+                            "--seed", "1321", "--check", "--nt", "4"],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0 and "pass" in r.stdout, r.stdout + r.stderr

@@ -1,0 +1,177 @@
+"""CPU: the C ABI loads and exports every declared symbol, host-side logic
+(generators, --nb resolution, argument checks, the CLI's parser) and the
+integer/float helpers shared by host and device code."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions(header: Path):
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(rmq_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(native):
+    names = declared_functions(ROOT / "include" / "rmq.h")
+    assert "rmq_build" in names and "rmq_query" in names and "rmq_free" in names
+    missing = [n for n in names if not hasattr(native, n)]
+    assert not missing, missing
+    from rtxrmq_gb300._native import SIGNATURES
+    assert sorted(SIGNATURES) == names
+
+
+def test_version_and_error_string(native):
+    assert b"sm_103a" in native.rmq_version()
+    import rtxrmq_gb300 as R
+    with pytest.raises(R.RMQError) as e:
+        R.bs_from_nb(0, 5)
+    assert e.value.code == -1 and "n=0" in str(e.value)
+
+
+@pytest.mark.parametrize("n,nb,bs", [(10**8, 512, 195312), (10**8, 8192, 12207), (100, 1000, 1),
+                                     (100, 3, 33), (7, 7, 1)])
+def test_bs_from_nb_matches_reference_cli(native, n, nb, bs):
+    """src/tools.h:129-132: nb = min(n, nb); bs = n / nb."""
+    import rtxrmq_gb300 as R
+    assert R.bs_from_nb(n, nb) == bs
+
+
+def test_null_handle_calls_fail_cleanly(native):
+    import ctypes as C
+    assert native.rmq_query(None, None, 1, None, None, None) == -1
+    assert native.rmq_free(None) == 0
+    h = C.c_void_p()
+    assert native.rmq_build(None, 10, 0, None, C.byref(h)) == -1
+    assert native.rmq_build(None, 0, 0, None, C.byref(h)) == -1
+    assert native.rmq_query_scan(None, 10, None, 1, None, None, None) == -1
+
+
+def test_generators_deterministic_and_prefix_stable(native):
+    import rtxrmq_gb300 as R
+    a = R.gen_values_uniform(100_000, 1321)
+    assert a.dtype == np.float32 and a.min() >= 0.0 and a.max() < 1.0
+    np.testing.assert_array_equal(a, R.gen_values_uniform(100_000, 1321))
+    np.testing.assert_array_equal(a[:777], R.gen_values_uniform(777, 1321))
+    q1 = R.gen_queries(5000, 10**6, -3, 9)
+    np.testing.assert_array_equal(q1[:100], R.gen_queries(100, 10**6, -3, 9))
+    # 24-bit resolution: values are multiples of 2^-24
+    assert np.all((a * 2**24) == np.floor(a * 2**24))
+
+
+@pytest.mark.parametrize("lr", [-1, -2, -3, -4, -5, 1, 32, 1024])
+def test_query_modes(native, lr):
+    import rtxrmq_gb300 as R
+    n = 10**6
+    Q = R.gen_queries(200_000, n, lr, 1321)
+    l, r = Q[:, 0].astype(np.int64), Q[:, 1].astype(np.int64)
+    assert (l >= 0).all() and (l <= r).all() and (r < n).all()
+    ln = r - l + 1
+    if lr > 0:
+        assert (ln == lr).all()
+    elif lr == -1:
+        assert abs(ln.mean() / (n / 2) - 1) < 0.01
+    else:
+        mu = {-2: 0.6 * np.log(n), -3: 0.3 * np.log(n), -4: np.log(n // 256),
+              -5: np.log(n // 32768)}[lr]
+        # median of a lognormal is exp(mu)
+        assert abs(np.median(ln) / np.exp(mu) - 1) < 0.02
+        assert abs(np.log(ln).std() - 0.3) < 0.02
+
+
+def test_config1_mean_length(native):
+    """Config n=1e6, q=2^20, lengths round(lognormal(0.3 ln n, 0.3)): mean
+    exp(mu + sigma^2/2) = 66.0 (the reference's truncating generator with
+    scale floor(n^0.3) gives 65.4)."""
+    import rtxrmq_gb300 as R
+    Q = R.gen_queries(1 << 20, 10**6, -3, 1321)
+    expect = np.exp(0.3 * np.log(1e6) + 0.3**2 / 2)
+    assert abs((Q[:, 1] - Q[:, 0] + 1).mean() - expect) < 0.3
+
+
+def test_value_generators(native):
+    import rtxrmq_gb300 as R
+    z = R.gen_values_normal(200_000, 5)
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+    k = R.gen_values_int(200_000, 256, 5)
+    assert set(np.unique(k)) == set(range(256))
+
+
+HELPER_TEST = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <cmath>
+#include "common.cuh"
+using namespace rmq;
+static unsigned long long rng = 88172645463325252ull;
+static unsigned next() { rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17; return (unsigned)rng; }
+static float f(unsigned b) { float x; std::memcpy(&x, &b, 4); return x; }
+int main() {
+  std::vector<unsigned> ds = {1,2,3,4,5,6,7,8,9,10,11,12,13,31,32,33,63,64,65,100,127,128,129,
+     1000,1023,1024,1025,4095,4096,4097,12207,32767,32768,32769,65535,65536,195312,1000000,
+     (1u<<30)-1, 1u<<30, (1u<<30)+1, 0x7fffffffu};
+  for (int i = 0; i < 2000; ++i) ds.push_back(1 + next() % 0x7fffffffu);
+  for (int i = 0; i < 2000; ++i) ds.push_back(1 + next() % 70000u);
+  for (unsigned d : ds) {
+    Div31 D = make_div31(d);
+    std::vector<unsigned> xs = {0u, 1u, d - 1, d, d + 1, 0x7fffffffu, 0x7ffffffeu};
+    for (unsigned k = 1; k < 40; ++k) { unsigned long long m = (unsigned long long)k * d;
+      if (m < 0x80000000ull) { xs.push_back((unsigned)m); xs.push_back((unsigned)m - 1); } }
+    for (unsigned long long m = d; m < 0x80000000ull; m *= 3) { xs.push_back((unsigned)m - 1); xs.push_back((unsigned)m); }
+    for (int i = 0; i < 2000; ++i) xs.push_back(next() & 0x7fffffffu);
+    for (unsigned x : xs) if (x <= 0x7fffffffu && div31(x, D) != x / d) {
+      std::printf("div31 mismatch d=%u x=%u got %u\n", d, x, div31(x, D)); return 1; }
+  }
+  // fkey: order preserving for float <, -0 == +0, NaN above +inf, funkey inverse
+  std::vector<unsigned> bs = {0u, 0x80000000u, 0x7f800000u, 0xff800000u, 1u, 0x80000001u,
+                              0x3f800000u, 0xbf800000u, 0x00800000u, 0x80800000u, 0x7f7fffffu, 0xff7fffffu};
+  for (int i = 0; i < 4000; ++i) { unsigned b = next(); if (!std::isnan(f(b))) bs.push_back(b); }
+  for (unsigned a : bs) {
+    if (funkey(fkey(a), a == 0x80000000u) != a) { std::printf("funkey %08x\n", a); return 1; }
+    for (unsigned b : bs) {
+      bool lt = f(a) < f(b), eq = f(a) == f(b);
+      if (lt != (fkey(a) < fkey(b)) || eq != (fkey(a) == fkey(b))) {
+        std::printf("fkey order %08x %08x\n", a, b); return 1; }
+    }
+  }
+  unsigned nanb[] = {0x7fc00000u, 0xffc00000u, 0x7f800001u, 0xffffffffu};
+  for (unsigned nb : nanb) if (fkey(nb) != 0xffffffffu || fkey(nb) <= fkey(0x7f800000u)) { std::printf("nan\n"); return 1; }
+  for (unsigned k = 1; k < 33; ++k) { unsigned x = (k == 32) ? 0xffffffffu : (1u << k) - 1;
+    if (ilog2(x) != (int)std::floor(std::log2((double)x))) { std::printf("ilog2 %u\n", x); return 1; } }
+  std::printf("ok\n");
+  return 0;
+}
+"""
+
+
+def test_device_helpers_on_host(tmp_path, native):
+    """common.cuh compiled for the host: exact magic division for every
+    31-bit dividend class, order-preserving float keys, ilog2."""
+    src = tmp_path / "t.cpp"
+    src.write_text(HELPER_TEST)
+    exe = tmp_path / "t"
+    cuda_inc = Path("/usr/local/cuda/include")
+    r = subprocess.run(["g++", "-O2", "-std=c++17", f"-I{ROOT / 'rtxrmq_gb300' / 'csrc'}",
+                        f"-I{cuda_inc}", str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr
+
+
+CLI = ROOT / "rtxrmq_gb300" / "_lib" / "rtxrmq"
+
+
+@pytest.mark.parametrize("args,code", [([], 1), (["0", "10", "1", "5"], 1), (["100", "10", "101", "5"], 1),
+                                       (["1000", "10", "-1", "0"], 2), (["1000", "10", "-1", "1"], 2),
+                                       (["1000", "10", "-1", "101"], 2), (["1000", "10", "-1", "3"], 2)])
+def test_cli_argument_errors(native, args, code):
+    """Argument errors and algorithms outside this engine exit before any
+    CUDA call (src/tools.h:76-95 checks)."""
+    r = subprocess.run([str(CLI), *args], capture_output=True, text=True, timeout=60)
+    assert r.returncode == code, r.stdout + r.stderr
