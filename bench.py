@@ -10,9 +10,10 @@ of each mode is the fastest of a sweep over 2^10..2^16.
 
 value      -- RMQ/s of the device-resident step (inputs already in HBM),
               timed with CUDA events on the launching stream.
-e2e        -- the same step through the C ABI with host buffers: pinned
-              queries copied in, results (values + indices) copied out,
-              all inside the timed region.
+e2e        -- the same step through the C ABI with host buffers
+              (rmq_query_host): the kernel reads the pinned host queries and
+              writes values + indices into pinned host memory over
+              NVLink-C2C, all inside the timed region.
 roofline   -- algorithmic HBM bytes per launch (query read + result write +
               one 32-byte sector per pre/suf lookup, 32 bytes per sector a
               block scan touches) / kernel time, against the measured copy
@@ -57,6 +58,14 @@ def parse():
     ap.add_argument("--q", type=int, default=N_QUERIES)
     ap.add_argument("--modes", default="all", help="comma list of lr values or 'all'")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--bs", type=int, default=0, help="fixed block size (skips the sweep)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end step")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-autograd", action="store_true")
+    ap.add_argument("--batch-arrays", type=int, default=4096)
+    ap.add_argument("--batch-q", type=int, default=1 << 26)
+    ap.add_argument("--diff-rows", type=int, default=256)
+    ap.add_argument("--diff-qpr", type=int, default=1 << 16)
     return ap.parse_args()
 
 
@@ -231,6 +240,133 @@ def run_reference(args, rank):
 
 # ---------------------------------------------------------------- GPU side
 
+def graph_of(fn, stream):
+    """Capture fn() once in a CUDA graph (after a warm run on a side stream)."""
+    import torch
+    s = torch.cuda.Stream()
+    s.wait_stream(stream)
+    with torch.cuda.stream(s):
+        fn()
+    stream.wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    torch.cuda.synchronize()
+    return g
+
+
+def bench_batched(args, dev, stream, barrier):
+    """Batched ragged config: 4096 arrays, lengths round(2^U), U ~ U[8,22],
+    2^26 queries proportional to length, lognormal(0.5 ln len, 0.4) lengths.
+    Step = build every array + answer every query."""
+    import torch
+
+    from rtxrmq_gb300 import workloads as W
+    from rtxrmq_gb300.batch import RMQBatch, autotune
+    t = time.perf_counter()
+    w = W.ragged(narrays=args.batch_arrays, total_q=args.batch_q, seed=SEED)
+    gen_s = time.perf_counter() - t
+    dV = torch.from_numpy(w.values).to(dev)
+    dQ = torch.from_numpy(w.queries).to(dev)
+    ov = torch.empty(w.total_q, dtype=torch.float32, device=dev)
+    oi = torch.empty(w.total_q, dtype=torch.int32, device=dev)
+    t = time.perf_counter()
+    cfg = autotune(w.starts, w.lengths, w.qstarts, w.qcounts, dV, dQ, reps=2,
+                   queries_host=w.queries, cache=None)
+    tune_s = time.perf_counter() - t
+    res = {"workload": "4096 arrays, len round(2^U) U~U[8,22], 2^26 queries proportional to "
+                       "length, query len lognormal(0.5 ln len, 0.4), values U[0,1)",
+           "arrays": int(len(w.lengths)), "elements": int(w.lengths.sum()), "queries": w.total_q,
+           "generate_s": gen_s, "autotune_s": tune_s,
+           "bucket_bs": {str(b): v for b, v in enumerate(cfg) if v}}
+    with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, cfg) as b:
+        info = b.info()
+        res["workspace_gb"] = info["workspace_bytes"] / 1e9
+        fn = lambda: b.run(dV, dQ, ov, oi)  # noqa: E731
+        ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
+        g = graph_of(fn, stream)
+        gms = time_steps(g.replay, args.steps, args.warmup, stream, barrier)
+        v1, i1 = ov.clone(), oi.clone()
+        pms = time_steps(lambda: b.run_per_array(dV, dQ, ov, oi), max(2, args.steps // 3), 1,
+                         stream, barrier)
+        match = bool(torch.equal(i1, oi) and torch.equal(v1.view(torch.int32), ov.view(torch.int32)))
+        del g
+    with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, None) as b:
+        dms = time_steps(lambda: b.run(dV, dQ, ov, oi), args.steps, 1, stream, barrier)
+    q = w.total_q
+    res.update({"batched_graph_rmq_s": q / (gms / 1e3), "batched_graph_ms": gms,
+                "batched_rmq_s": q / (ms / 1e3), "batched_ms": ms,
+                "per_array_rmq_s": q / (pms / 1e3), "per_array_ms": pms,
+                "speedup_vs_per_array": pms / gms,
+                "default_bs_rmq_s": q / (dms / 1e3),
+                "per_array_matches_batched": match,
+                "launches_per_step": {"batched": 1, "per_array": "one build + level + query "
+                                      "launch sequence per array"}})
+    del dV, dQ, ov, oi
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_autograd(args, dev, stream, barrier):
+    """Differentiable config: 256 rows N(0,1), lengths U[2^14, 2^20], 2^16
+    ranges per row with lengths lognormal(0.4 ln len, 0.5); grad_out N(0,1).
+    Forward and forward+backward each captured in a CUDA graph."""
+    import torch
+
+    from rtxrmq_gb300 import workloads as W
+    from rtxrmq_gb300.autograd import RaggedRangeMin
+    from rtxrmq_gb300.batch import autotune
+    d = W.differentiable_rows(nrows=args.diff_rows, q_per_row=args.diff_qpr, seed=SEED)
+    x = torch.from_numpy(d.values).to(dev)
+    dQ = torch.from_numpy(d.queries).to(dev)
+    gout_h = np.random.default_rng(SEED).standard_normal(d.total_q).astype(np.float32)
+    go = torch.from_numpy(gout_h).to(dev)
+    cfg = autotune(d.starts, d.lengths, d.qstarts, d.qcounts, x, dQ, reps=2,
+                   queries_host=d.queries, cache=None)
+    m = RaggedRangeMin(d.lengths, d.qcounts, cfg)
+    xg = x.clone().requires_grad_(True)
+
+    def fwd():
+        with torch.no_grad():
+            return m(x, dQ)
+
+    def fwd_bwd():
+        xg.grad = None
+        y, _ = m(xg, dQ)
+        y.backward(go)
+
+    fwd_bwd()  # allocate grad once outside capture
+    gf = graph_of(fwd, stream)
+    xg.grad = None
+    gb = graph_of(fwd_bwd, stream)
+    fms = time_steps(gf.replay, args.steps, args.warmup, stream, barrier)
+    bms = time_steps(gb.replay, args.steps, args.warmup, stream, barrier)
+    # full-size check of the gradient against an FP64 scatter of the same argmins
+    y, idx = fwd()
+    torch.cuda.synchronize()
+    gidx = idx.cpu().numpy().astype(np.int64) + np.repeat(d.starts, d.qcounts)
+    g64 = np.zeros(d.span, np.float64)
+    np.add.at(g64, gidx, gout_h.astype(np.float64))
+    scale = np.zeros(d.span, np.float64)  # sum of |contributions| per element
+    np.add.at(scale, gidx, np.abs(gout_h.astype(np.float64)))
+    gb.replay()
+    torch.cuda.synchronize()
+    g = xg.grad.cpu().numpy().astype(np.float64)
+    nz = scale > 0
+    rel = float((np.abs(g[nz] - g64[nz]) / scale[nz]).max()) if nz.any() else 0.0
+    zero_ok = bool(np.all(g[~nz] == 0))
+    q = d.total_q
+    res = {"workload": "256 rows N(0,1), len U[2^14,2^20], 2^16 ranges/row, len lognormal("
+                       "0.4 ln len, 0.5), grad_out N(0,1)",
+           "elements": d.span, "queries": q, "bucket_bs": {str(b): v for b, v in enumerate(cfg) if v},
+           "fwd_ms": fms, "fwd_bwd_ms": bms, "fwd_bwd_over_fwd": bms / fms,
+           "fwd_rmq_s": q / (fms / 1e3), "fwd_bwd_rmq_s": q / (bms / 1e3),
+           "graph_captured": True, "grad_max_rel_err_vs_fp64": rel, "grad_zero_elsewhere": zero_ok}
+    del gf, gb, x, xg, dQ, go
+    torch.cuda.empty_cache()
+    return res
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -273,7 +409,7 @@ def main():
             dQ = torch.from_numpy(Q).to(dev)
             sweep = {}
             best = None
-            for bs in BS_SWEEP:
+            for bs in ([args.bs] if args.bs else BS_SWEEP):
                 ix = R.RMQIndex(dA, bs)
                 fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
                 ms = time_steps(fn, 3, 1, stream, barrier)
@@ -300,18 +436,16 @@ def main():
                    "alg_bytes_per_step": alg_bytes,
                    "achieved_gbs": alg_bytes / (ms / 1e3) / 1e9,
                    "info": ix.info()}
-            if lr == -1:
-                # end to end through the C ABI with host buffers
+            if lr == -1 and not args.no_e2e:
+                # end to end through the C ABI with host buffers: rmq_query_host
+                # reads the pinned queries and writes the pinned results in
+                # place over NVLink-C2C inside the timed region
                 hQ = torch.from_numpy(Q).pin_memory()
                 hV = torch.empty(q, dtype=torch.float32).pin_memory()
                 hI = torch.empty(q, dtype=torch.int32).pin_memory()
-                dQ2 = torch.empty_like(dQ)
 
                 def e2e():
-                    dQ2.copy_(hQ, non_blocking=True)
-                    ix.query(dQ2, out_val=out_v, out_idx=out_i)
-                    hV.copy_(out_v, non_blocking=True)
-                    hI.copy_(out_i, non_blocking=True)
+                    ix.query_host(hQ, hV, hI)
 
                 e2e_ms = time_steps(e2e, args.steps, args.warmup, stream, barrier)
                 if world > 1:
@@ -319,16 +453,25 @@ def main():
                     dist.all_reduce(tt, op=dist.ReduceOp.MAX)
                     e2e_ms = float(tt.item())
                 torch.cuda.synchronize()
-                ok = (np.array_equal(hI[:4096].numpy(), out_i[:4096].cpu().numpy()))
+                ix.query(dQ, out_val=out_v, out_idx=out_i)
+                torch.cuda.synchronize()
+                ok = (np.array_equal(hI.numpy(), out_i.cpu().numpy()) and
+                      np.array_equal(hV.numpy().view(np.uint32), out_v.cpu().numpy().view(np.uint32)))
                 res["e2e"] = {"value": world * q / (e2e_ms / 1e3), "unit": "RMQ/s",
                               "h2d_bytes_per_step": int(Q.nbytes),
                               "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
-                              "ms_per_step": e2e_ms, "copy_check": bool(ok)}
+                              "ms_per_step": e2e_ms, "path": "rmq_query_host, pinned host buffers",
+                              "matches_device_path": bool(ok)}
+                del hQ, hV, hI
+            if lr == -1:
                 headline = (name, lr, Q, bs)
-                del hQ, hV, hI, dQ2
             ix.close()
             results[name] = res
             del dQ
+        del dA
+        torch.cuda.empty_cache()
+        batched = None if args.skip_batched else bench_batched(args, dev, stream, barrier)
+        autograd = None if args.skip_autograd else bench_autograd(args, dev, stream, barrier)
     clocks = sampler.summary()
 
     if rank != 0:
@@ -358,6 +501,8 @@ def main():
                      "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
         "clocks": clocks,
         "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
+        "batched": batched,
+        "autograd": autograd,
     }
     if not args.no_cpu and world == 1:
         cbs = cpu_bs(n)

@@ -90,6 +90,22 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
 int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
               float *d_val, int32_t *d_idx, rmq_stream_t stream);
 
+/*
+ * rmq_query with host-side buffers: h_queries, h_val, h_idx live in host
+ * memory that the GPU can address -- page-locked memory (cudaHostAlloc,
+ * cudaHostRegister) or, on systems where the device reads pageable memory
+ * (Grace-Blackwell: cudaDevAttrPageableMemoryAccess), any host memory; device
+ * pointers are accepted as well. The query kernel reads the queries and
+ * writes the results in place over the host link (NVLink-C2C on GB300), so
+ * no staging copies are made and nothing is allocated. Stream ordered: the
+ * results are in the host buffers once `stream` has been synchronised.
+ * A buffer the device cannot address is rejected with RMQ_EINVAL.
+ * This is the end-to-end form of the reference's timed loop plus its
+ * copy-out (src/rtx.h:150-159).
+ */
+int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q,
+                   float *h_val, int32_t *h_idx, rmq_stream_t stream);
+
 /* Release everything the handle owns. NULL is accepted. */
 int rmq_free(rmq_handle_t *h);
 
@@ -123,6 +139,87 @@ int rmq_bs_from_nb(int64_t n, int64_t nb, int64_t *bs);
 int rmq_query_scan(const float *d_vals, int64_t n, const int32_t *d_queries,
                    int64_t q, float *d_val, int32_t *d_idx,
                    rmq_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Batched ragged form: many independent arrays of uneven length, each with
+ * its own queries, built and answered by ONE persistent cooperative kernel
+ * launch (no allocation per run, so a run can be captured in a CUDA graph).
+ * The reference has no batched form: rtx_rmq<T> (src/rtx.h:24-177) serves
+ * one array per call; rmq_batch_run_per_array is that plain path, one build
+ * and one query launch sequence per array, over the same plan.
+ *
+ * Array i holds d_vals[h_starts[i] .. h_starts[i] + h_lengths[i]) and owns
+ * the queries d_queries[h_qstarts[i] .. h_qstarts[i] + h_qcounts[i]) (int32
+ * pairs in array-local coordinates); outputs are written at the queries'
+ * positions, indices array-local. Arrays and query ranges may sit anywhere
+ * in their buffers (gaps allowed). Arrays are grouped into size buckets
+ * floor(log2 length); h_bucket_bs[bucket] (RMQ_BATCH_BUCKETS entries, or
+ * NULL; <= 0 means default) is the block size of that bucket, as chosen by
+ * rmq_batch_autotune.
+ * ---------------------------------------------------------------------- */
+#define RMQ_BATCH_BUCKETS 32
+
+typedef struct rmq_batch rmq_batch_t;
+
+typedef struct rmq_batch_info {
+    int32_t narrays;
+    int32_t max_levels;
+    int64_t values_span;      /* one past the last value any array uses   */
+    int64_t queries_span;     /* one past the last query any array owns   */
+    int64_t workspace_bytes;  /* prefix/suffix minima and sparse tables   */
+    int64_t device_bytes;     /* all device memory owned by the plan      */
+    int32_t build_items;
+    int32_t query_items;
+    int32_t bucket_bs[RMQ_BATCH_BUCKETS];
+} rmq_batch_info_t;
+
+/* Plan a batch (host metadata in, device workspace allocated here). */
+int rmq_batch_create(int32_t narrays, const int64_t *h_starts,
+                     const int64_t *h_lengths, const int64_t *h_qstarts,
+                     const int64_t *h_qcounts, const int32_t *h_bucket_bs,
+                     rmq_batch_t **out);
+
+/* Build every array and answer every query: one cooperative launch. */
+int rmq_batch_run(rmq_batch_t *b, const float *d_vals,
+                  const int32_t *d_queries, float *d_val, int32_t *d_idx,
+                  rmq_stream_t stream);
+
+/* The same results through the plain path: per array one rmq_build-style
+ * launch sequence and one rmq_query-style launch (comparison baseline). */
+int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals,
+                            const int32_t *d_queries, float *d_val,
+                            int32_t *d_idx, rmq_stream_t stream);
+
+/*
+ * Backward of the batched range-min: d_grad_vals[start(i) + d_idx[q]] +=
+ * d_grad_out[q] for every query q of array i (fp32 atomics, so the order of
+ * additions is not deterministic). accumulate == 0 zeroes
+ * d_grad_vals[0 .. values_span) first. Indices < 0 (invalid queries) are
+ * skipped. No allocation.
+ */
+int rmq_batch_scatter_grad(const rmq_batch_t *b, const int32_t *d_idx,
+                           const float *d_grad_out, float *d_grad_vals,
+                           int32_t accumulate, rmq_stream_t stream);
+
+int rmq_batch_info(const rmq_batch_t *b, rmq_batch_info_t *info);
+/* Invalid queries seen by this plan; synchronises `stream`. */
+int rmq_batch_invalid_count(const rmq_batch_t *b, rmq_stream_t stream,
+                            int64_t *count);
+int rmq_batch_free(rmq_batch_t *b);
+
+/*
+ * Per-size-bucket block-size autotuner: for every bucket present, times a
+ * batch of that bucket's arrays and queries with each candidate block size
+ * (64 .. 65536, up to twice the bucket's largest length) over `reps` runs
+ * and writes the fastest to h_bucket_bs[bucket] (0 for absent buckets).
+ * Uses d_val / d_idx as scratch outputs; allocates and frees temporary plans.
+ */
+int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts,
+                       const int64_t *h_lengths, const int64_t *h_qstarts,
+                       const int64_t *h_qcounts, const float *d_vals,
+                       const int32_t *d_queries, float *d_val, int32_t *d_idx,
+                       int32_t reps, rmq_stream_t stream,
+                       int32_t *h_bucket_bs);
 
 /*
  * Host-side synthetic inputs (OpenMP; the output does not depend on the

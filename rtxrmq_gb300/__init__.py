@@ -105,6 +105,27 @@ class RMQIndex:
                                _stream_handle(stream)))
         return out_val, out_idx
 
+    def query_host(self, queries, out_val=None, out_idx=None, stream=None) -> None:
+        """rmq_query_host: host-side buffers (CPU tensors or numpy arrays;
+        page-locked memory, or any memory where the device reads pageable
+        memory) read and written in place by the kernel. Results are valid
+        after the stream is synchronised."""
+        def hptr(x):
+            if x is None:
+                return None
+            if hasattr(x, "data_ptr"):
+                if not x.is_contiguous():
+                    raise ValueError("expected a contiguous buffer")
+                return x.data_ptr()
+            if not x.flags["C_CONTIGUOUS"]:
+                raise ValueError("expected a contiguous buffer")
+            return x.ctypes.data
+        q = len(queries)
+        if tuple(queries.shape[1:]) != (2,):
+            raise ValueError("queries must have shape [q, 2]")
+        check(load().rmq_query_host(self._h, hptr(queries), q, hptr(out_val), hptr(out_idx),
+                                    _stream_handle(stream)))
+
     def invalid_count(self, stream=None) -> int:
         v = C.c_int64()
         check(load().rmq_invalid_count(self._h, _stream_handle(stream), C.byref(v)))

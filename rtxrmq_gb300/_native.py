@@ -35,12 +35,23 @@ class rmq_info_t(C.Structure):
                 ("aligned", C.c_int32), ("table_bytes", C.c_int64), ("struct_bytes", C.c_int64)]
 
 
+RMQ_BATCH_BUCKETS = 32
+
+
+class rmq_batch_info_t(C.Structure):
+    _fields_ = [("narrays", C.c_int32), ("max_levels", C.c_int32), ("values_span", C.c_int64),
+                ("queries_span", C.c_int64), ("workspace_bytes", C.c_int64),
+                ("device_bytes", C.c_int64), ("build_items", C.c_int32),
+                ("query_items", C.c_int32), ("bucket_bs", C.c_int32 * RMQ_BATCH_BUCKETS)]
+
+
 _vp, _i64, _i32, _u64, _dbl = C.c_void_p, C.c_int64, C.c_int32, C.c_uint64, C.c_double
 
 # name -> (restype, argtypes); every symbol include/rmq.h declares
 SIGNATURES = {
     "rmq_build": (C.c_int, [_vp, _i64, _i64, _vp, C.POINTER(_vp)]),
     "rmq_query": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "rmq_query_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "rmq_free": (C.c_int, [_vp]),
     "rmq_info": (C.c_int, [_vp, C.POINTER(rmq_info_t)]),
     "rmq_invalid_count": (C.c_int, [_vp, _vp, C.POINTER(_i64)]),
@@ -48,6 +59,14 @@ SIGNATURES = {
     "rmq_version": (C.c_char_p, []),
     "rmq_bs_from_nb": (C.c_int, [_i64, _i64, C.POINTER(_i64)]),
     "rmq_query_scan": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
+    "rmq_batch_create": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "rmq_batch_run": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "rmq_batch_run_per_array": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "rmq_batch_scatter_grad": (C.c_int, [_vp, _vp, _vp, _vp, _i32, _vp]),
+    "rmq_batch_info": (C.c_int, [_vp, C.POINTER(rmq_batch_info_t)]),
+    "rmq_batch_invalid_count": (C.c_int, [_vp, _vp, C.POINTER(_i64)]),
+    "rmq_batch_free": (C.c_int, [_vp]),
+    "rmq_batch_autotune": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp]),
     "rmq_gen_values_uniform": (C.c_int, [_vp, _i64, _u64]),
     "rmq_gen_values_normal": (C.c_int, [_vp, _i64, _dbl, _dbl, _u64]),
     "rmq_gen_values_int": (C.c_int, [_vp, _i64, _i32, _u64]),

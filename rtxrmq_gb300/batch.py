@@ -1,0 +1,202 @@
+"""Batched ragged RMQ over the C ABI (rmq_batch_* in include/rmq.h).
+
+Thousands of independent float32 arrays of uneven length, each with its own
+(l, r) queries, are built and answered by one persistent cooperative kernel
+launch. ``run_per_array`` produces the same results through the plain path
+(one build + one query launch sequence per array) for comparison.
+``autotune`` picks the block size of every size bucket (floor(log2 length))
+by timing the candidates on the actual arrays and queries, and caches the
+choice per GPU model, bucket and query-length class.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+from ._native import RMQ_BATCH_BUCKETS, check, load, rmq_batch_info_t
+
+__all__ = ["RMQBatch", "autotune", "bucket_of", "DEFAULT_CACHE"]
+
+DEFAULT_CACHE = Path(os.environ.get("RTXRMQ_AUTOTUNE_CACHE",
+                                    Path.home() / ".cache" / "rtxrmq_gb300" / "autotune.json"))
+
+
+def _i64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int64))
+
+
+def bucket_of(n) -> np.ndarray:
+    n = np.asarray(n, dtype=np.int64)
+    return np.where(n <= 1, 0, np.floor(np.log2(np.maximum(n, 1))).astype(np.int64))
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream if isinstance(stream, int) else stream.cuda_stream
+
+
+def _dptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+class RMQBatch:
+    """A planned batch: array i is values[starts[i] : starts[i] + lengths[i]]
+    and owns queries[qstarts[i] : qstarts[i] + qcounts[i]] (array-local
+    int32 (l, r) pairs). ``bucket_bs`` maps size bucket -> block size."""
+
+    def __init__(self, starts: Sequence[int], lengths: Sequence[int], qstarts: Sequence[int],
+                 qcounts: Sequence[int], bucket_bs: Optional[Sequence[int]] = None):
+        self.starts, self.lengths = _i64(starts), _i64(lengths)
+        self.qstarts, self.qcounts = _i64(qstarts), _i64(qcounts)
+        n = len(self.starts)
+        if not (len(self.lengths) == len(self.qstarts) == len(self.qcounts) == n):
+            raise ValueError("starts, lengths, qstarts, qcounts must have the same length")
+        cfg = None
+        if bucket_bs is not None:
+            cfg = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
+            b = np.asarray(bucket_bs, dtype=np.int32)[:RMQ_BATCH_BUCKETS]
+            cfg[:len(b)] = b
+        self._cfg = cfg
+        self._h = C.c_void_p()
+        check(load().rmq_batch_create(n, self.starts.ctypes.data, self.lengths.ctypes.data,
+                                      self.qstarts.ctypes.data, self.qcounts.ctypes.data,
+                                      None if cfg is None else cfg.ctypes.data, C.byref(self._h)))
+
+    def _out(self, queries, out_val, out_idx, values: bool, indices: bool):
+        import torch
+        q = queries.shape[0]
+        if values and out_val is None:
+            out_val = torch.empty(q, dtype=torch.float32, device=queries.device)
+        if indices and out_idx is None:
+            out_idx = torch.empty(q, dtype=torch.int32, device=queries.device)
+        return (out_val if values else None), (out_idx if indices else None)
+
+    def run(self, vals, queries, out_val=None, out_idx=None, *, values=True, indices=True,
+            stream=None):
+        """Build + answer everything in one cooperative launch."""
+        v, i = self._out(queries, out_val, out_idx, values, indices)
+        check(load().rmq_batch_run(self._h, _dptr(vals), _dptr(queries), _dptr(v), _dptr(i),
+                                   _stream(stream)))
+        return v, i
+
+    def run_per_array(self, vals, queries, out_val=None, out_idx=None, *, values=True,
+                      indices=True, stream=None):
+        """Same results through the plain path, one launch sequence per array."""
+        v, i = self._out(queries, out_val, out_idx, values, indices)
+        check(load().rmq_batch_run_per_array(self._h, _dptr(vals), _dptr(queries), _dptr(v),
+                                             _dptr(i), _stream(stream)))
+        return v, i
+
+    def scatter_grad(self, idx, grad_out, grad_vals, accumulate: bool = False, stream=None):
+        check(load().rmq_batch_scatter_grad(self._h, _dptr(idx), _dptr(grad_out),
+                                            _dptr(grad_vals), int(bool(accumulate)),
+                                            _stream(stream)))
+        return grad_vals
+
+    def info(self) -> dict:
+        inf = rmq_batch_info_t()
+        check(load().rmq_batch_info(self._h, C.byref(inf)))
+        d = {k: getattr(inf, k) for k, _ in rmq_batch_info_t._fields_ if k != "bucket_bs"}
+        d["bucket_bs"] = list(inf.bucket_bs)
+        return d
+
+    def invalid_count(self, stream=None) -> int:
+        v = C.c_int64()
+        check(load().rmq_batch_invalid_count(self._h, _stream(stream), C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            check(load().rmq_batch_free(self._h))
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _cache_keys(lengths, qstarts, qcounts, queries_host) -> dict:
+    """bucket -> key 'b<bucket>_q<log2 mean query length>'."""
+    keys = {}
+    bk = bucket_of(lengths)
+    for b in np.unique(bk):
+        members = np.nonzero(bk == b)[0]
+        if queries_host is None:
+            qcls = "na"
+        else:
+            tot, cnt = 0.0, 0
+            for i in members[:64]:
+                s, c = int(qstarts[i]), int(min(qcounts[i], 4096))
+                if c:
+                    q = queries_host[s:s + c]
+                    tot += float((q[:, 1] - q[:, 0] + 1).sum())
+                    cnt += c
+            qcls = str(int(round(np.log2(max(tot / max(cnt, 1), 1.0)))))
+        keys[int(b)] = f"b{int(b)}_q{qcls}"
+    return keys
+
+
+def autotune(starts, lengths, qstarts, qcounts, vals, queries, *, reps: int = 3,
+             queries_host: Optional[np.ndarray] = None, cache: Optional[Path] = DEFAULT_CACHE,
+             stream=None) -> list:
+    """Per-bucket block sizes for this batch (RMQ_BATCH_BUCKETS entries).
+
+    Cached results (per GPU model and bucket/query-length key) are reused;
+    missing buckets are timed by rmq_batch_autotune on the real data."""
+    import torch
+    starts, lengths = _i64(starts), _i64(lengths)
+    qstarts, qcounts = _i64(qstarts), _i64(qcounts)
+    dev = torch.cuda.get_device_name()
+    keys = _cache_keys(lengths, qstarts, qcounts, queries_host)
+    table = {}
+    if cache is not None and Path(cache).exists():
+        try:
+            table = json.loads(Path(cache).read_text()).get(dev, {})
+        except (OSError, ValueError):
+            table = {}
+    out = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
+    missing = [b for b, k in keys.items() if k not in table]
+    for b, k in keys.items():
+        if k in table:
+            out[b] = int(table[k])
+    if missing:
+        sel = np.nonzero(np.isin(bucket_of(lengths), missing))[0]
+        res = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
+        qn = int(queries.shape[0])
+        sv = torch.empty(qn, dtype=torch.float32, device=queries.device)
+        si = torch.empty(qn, dtype=torch.int32, device=queries.device)
+        s_, l_, qs_, qc_ = (np.ascontiguousarray(x[sel]) for x in (starts, lengths, qstarts, qcounts))
+        check(load().rmq_batch_autotune(len(sel), s_.ctypes.data, l_.ctypes.data, qs_.ctypes.data,
+                                        qc_.ctypes.data, _dptr(vals), _dptr(queries), _dptr(sv),
+                                        _dptr(si), int(reps), _stream(stream), res.ctypes.data))
+        for b in missing:
+            out[b] = res[b]
+            table[keys[b]] = int(res[b])
+        if cache is not None:
+            try:
+                Path(cache).parent.mkdir(parents=True, exist_ok=True)
+                full = json.loads(Path(cache).read_text()) if Path(cache).exists() else {}
+                full[dev] = table
+                Path(cache).write_text(json.dumps(full, indent=1, sort_keys=True))
+            except (OSError, ValueError):
+                pass
+    return [int(x) for x in out]

@@ -178,6 +178,59 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float 
     return RMQ_OK;
 }
 
+// Device-usable address of a buffer the caller calls "host" memory, or null
+// if the current device cannot address it.
+static const void *device_view(const void *p, bool *ok) {
+    *ok = false;
+    if (!p) {
+        *ok = true;
+        return nullptr;
+    }
+    cudaPointerAttributes at;
+    cudaError_t err = cudaPointerGetAttributes(&at, p);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        *ok = true;
+        return p;
+    }
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) {
+        *ok = true;
+        return at.devicePointer;
+    }
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+        pageable) {
+        *ok = true;
+        return p;
+    }
+    cudaGetLastError();
+    return nullptr;
+}
+
+int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, float *h_val,
+                   int32_t *h_idx, rmq_stream_t stream) {
+    g_err[0] = '\0';
+    if (!h) return set_error(RMQ_EINVAL, "rmq_query_host: handle is NULL");
+    if (q < 0) return set_error(RMQ_EINVAL, "rmq_query_host: q=%lld < 0", (long long)q);
+    if (q == 0) return RMQ_OK;
+    if (!h_queries) return set_error(RMQ_EINVAL, "rmq_query_host: h_queries is NULL");
+    if (!h_val && !h_idx) return set_error(RMQ_EINVAL, "rmq_query_host: both outputs are NULL");
+    bool okq, okv, oki;
+    const void *dq = device_view(h_queries, &okq);
+    void *dv = const_cast<void *>(device_view(h_val, &okv));
+    void *di = const_cast<void *>(device_view(h_idx, &oki));
+    if (!okq || !okv || !oki)
+        return set_error(RMQ_EINVAL,
+                         "rmq_query_host: a buffer is not addressable by the device "
+                         "(page-lock it with cudaHostRegister or allocate it with cudaHostAlloc)");
+    return rmq_query(h, static_cast<const int32_t *>(dq), q, static_cast<float *>(dv),
+                     static_cast<int32_t *>(di), stream);
+}
+
 int rmq_free(rmq_handle_t *h) {
     g_err[0] = '\0';
     if (!h) return RMQ_OK;

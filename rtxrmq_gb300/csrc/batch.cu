@@ -1,0 +1,523 @@
+// batch.cu -- many independent arrays of uneven length and their query sets
+// answered by one persistent, cooperative launch (build + query), the same
+// work as one plain build/query launch sequence per array, the gradient
+// scatter of the differentiable range-min, and the per-size-bucket block-size
+// autotuner.
+//
+// The reference has no batched form: rtx_rmq<T> (src/rtx.h:24-177) builds one
+// structure for one array and launches one optixLaunch per batch of queries.
+//
+// Persistent kernel, three phases separated by grid-wide barriers of a
+// cooperative launch (all CTAs are co-resident, guaranteed by the launch):
+//   A  build items (array, unit): prefix/suffix minima + block minima,
+//      build_impl.cuh, the plain builder's CTA body;
+//   B  sparse-table levels 1..L-1 of every array, one level per barrier,
+//      items (array, level, first entry, count);
+//   C  query items (array, first query, count), query_impl.cuh.
+// Work lists are built on the host once per plan, so a run allocates nothing
+// and can be captured in a CUDA graph.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/rmq.h"
+#include "build_impl.cuh"
+#include "engine.h"
+#include "query_impl.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace rmq {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kQPT = 2;
+constexpr uint32_t kQueryChunk = 2048;  // queries per query item
+constexpr uint32_t kLevelChunk = 4096;  // sparse-table entries per level item
+constexpr int kMaxLevels = 32;
+
+struct BatchArray {
+    int64_t off;    // first value in the buffer
+    int64_t qoff;   // first query
+    int64_t pre;    // workspace entry offset of pre[]; suf[] follows at pre + n
+    int64_t st;     // workspace entry offset of the sparse table
+    uint32_t n, bs, nb, levels;
+    UnitLayout U;
+    Div31 dv;
+};
+
+struct BatchParams {
+    const float *A;
+    int64_t limit;
+    const int2 *Q;
+    float *val;
+    int32_t *idx;
+    unsigned long long *invalid;
+    Entry *ws;
+    const BatchArray *arrays;
+    const uint2 *build;
+    int32_t nbuild;
+    const uint4 *lvl;
+    int32_t maxlev;
+    int32_t lvl_start[kMaxLevels + 1];
+    const uint4 *qitems;
+    int32_t nqitems;
+};
+
+__device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchArray &a) {
+    V1View v;
+    v.A = P.A;
+    v.off = a.off;
+    v.limit = P.limit;
+    v.n = a.n;
+    v.bs = a.bs;
+    v.nb = a.nb;
+    v.dv = a.dv;
+    v.pre = P.ws + a.pre;
+    v.suf = P.ws + a.pre + a.n;
+    v.st = P.ws + a.st;
+    return v;
+}
+
+template <bool ALIGNED>
+__global__ void __launch_bounds__(kThreads) batch_kernel(BatchParams P) {
+    __shared__ Entry stage[kStageEntries];
+    __shared__ uint64_t s_warp[kBuildWarps];
+    cg::grid_group grid = cg::this_grid();
+
+    // A: units
+    for (int32_t it = blockIdx.x; it < P.nbuild; it += gridDim.x) {
+        const uint2 w = P.build[it];
+        const BatchArray a = P.arrays[w.x];
+        UnitJob J;
+        J.A = P.A;
+        J.off = a.off;
+        J.limit = P.limit;
+        J.n = a.n;
+        J.bs = a.bs;
+        J.U = a.U;
+        J.dv = a.dv;
+        J.pre = P.ws + a.pre;
+        J.suf = P.ws + a.pre + a.n;
+        J.bmin = P.ws + a.st;
+        build_unit<ALIGNED>(J, w.y, stage, s_warp);
+    }
+    grid.sync();
+
+    // B: sparse-table levels
+    for (int k = 1; k < P.maxlev; ++k) {
+        for (int32_t it = P.lvl_start[k] + blockIdx.x; it < P.lvl_start[k + 1]; it += gridDim.x) {
+            const uint4 w = P.lvl[it];
+            const BatchArray &a = P.arrays[w.x];
+            const Entry *prev = P.ws + a.st + static_cast<int64_t>(k - 1) * a.nb;
+            Entry *cur = P.ws + a.st + static_cast<int64_t>(k) * a.nb;
+            const uint32_t half = 1u << (k - 1);
+            for (uint32_t j = w.z + threadIdx.x; j < w.z + w.w; j += kThreads)
+                cur[j] = better(prev[j], prev[j + half]);
+        }
+        grid.sync();
+    }
+
+    // C: queries
+    for (int32_t it = blockIdx.x; it < P.nqitems; it += gridDim.x) {
+        const uint4 w = P.qitems[it];
+        const BatchArray a = P.arrays[w.x];
+        const V1View v = batch_view(P, a);
+        QueryOut o;
+        o.Q = P.Q + a.qoff;
+        o.val = P.val ? P.val + a.qoff : nullptr;
+        o.idx = P.idx ? P.idx + a.qoff : nullptr;
+        o.invalid = P.invalid;
+        answer_range<ALIGNED, kQPT>(v, o, w.y, static_cast<int64_t>(w.y) + w.z);
+    }
+}
+
+// grad_vals[off(a) + idx[q]] += grad_out[q] for every query q of array a
+__global__ void __launch_bounds__(kThreads)
+scatter_grad_kernel(const BatchArray *arrays, const uint4 *qitems, int32_t nqitems,
+                    const int32_t *idx, const float *gout, float *gvals) {
+    for (int32_t it = blockIdx.x; it < nqitems; it += gridDim.x) {
+        const uint4 w = qitems[it];
+        const int64_t qoff = arrays[w.x].qoff + w.y;
+        const int64_t off = arrays[w.x].off;
+        for (uint32_t j = threadIdx.x; j < w.z; j += kThreads) {
+            const int32_t li = idx[qoff + j];
+            if (li >= 0) atomicAdd(gvals + off + li, gout[qoff + j]);
+        }
+    }
+}
+
+int g_batch_per_sm[2] = {0, 0};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+}  // namespace rmq
+
+using namespace rmq;
+
+struct rmq_batch {
+    int32_t narrays;
+    int64_t limit;       // one past the last value any array uses
+    int64_t total_q;     // one past the last query any array uses
+    int device;
+    std::vector<BatchArray> h_arrays;
+    std::vector<uint4> h_qitems;
+    void *mem;           // one device allocation: metadata, work lists, workspace, counter
+    size_t mem_bytes;
+    size_t ws_bytes;
+    BatchParams P;       // device pointers filled, per-run fields left empty
+    int32_t bucket_bs[RMQ_BATCH_BUCKETS];
+};
+
+namespace {
+
+int bucket_of(int64_t n) { return n <= 1 ? 0 : ilog2(static_cast<uint32_t>(n)); }
+
+int64_t default_bs(int64_t n) {
+    // short arrays: one block per 1024 elements; long arrays: 4096
+    return n <= (1 << 14) ? 1024 : 4096;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
+                     const int64_t *h_qstarts, const int64_t *h_qcounts,
+                     const int32_t *h_bucket_bs, rmq_batch_t **out) {
+    if (!out) return set_error(RMQ_EINVAL, "rmq_batch_create: out is NULL");
+    *out = nullptr;
+    if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts)
+        return set_error(RMQ_EINVAL, "rmq_batch_create: narrays must be > 0 and arrays non-NULL");
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+
+    rmq_batch_t *b = new (std::nothrow) rmq_batch_t;
+    if (!b) return set_error(RMQ_ENOMEM, "rmq_batch_create: host allocation failed");
+    b->narrays = narrays;
+    b->device = dev.device;
+    b->limit = 0;
+    b->total_q = 0;
+    b->mem = nullptr;
+    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i)
+        b->bucket_bs[i] = h_bucket_bs && h_bucket_bs[i] > 0 ? h_bucket_bs[i] : 0;
+
+    std::vector<uint2> build;
+    std::vector<std::vector<uint4>> lvl(kMaxLevels);
+    int64_t ws_entries = 0;
+    int32_t maxlev = 1;
+    b->h_arrays.resize(narrays);
+    for (int32_t i = 0; i < narrays; ++i) {
+        const int64_t n = h_lengths[i], s = h_starts[i];
+        const int64_t qs = h_qstarts[i], qc = h_qcounts[i];
+        if (n <= 0 || n > 0x7fffffffLL || s < 0 || qs < 0 || qc < 0 || qc > 0xffffffffLL) {
+            delete b;
+            return set_error(RMQ_EINVAL,
+                             "rmq_batch_create: array %d has start=%lld length=%lld qstart=%lld "
+                             "qcount=%lld (need length in [1, 2^31-1], others >= 0)",
+                             i, (long long)s, (long long)n, (long long)qs, (long long)qc);
+        }
+        int64_t bs = b->bucket_bs[bucket_of(n)];
+        if (bs <= 0) bs = default_bs(n);
+        if (bs > n) bs = n;
+        BatchArray &a = b->h_arrays[i];
+        a.off = s;
+        a.qoff = qs;
+        a.n = static_cast<uint32_t>(n);
+        a.bs = static_cast<uint32_t>(bs);
+        a.nb = static_cast<uint32_t>((n + bs - 1) / bs);
+        a.levels = st_levels(a.nb);
+        a.U = make_unit_layout(a.bs, a.nb);
+        a.dv = make_div31(a.bs);
+        a.pre = ws_entries;
+        ws_entries += 2 * n;
+        a.st = ws_entries;
+        ws_entries += static_cast<int64_t>(a.nb) * a.levels;
+        ws_entries = (ws_entries + 31) & ~int64_t(31);  // 256-byte alignment per array
+        b->limit = std::max(b->limit, s + n);
+        b->total_q = std::max(b->total_q, qs + qc);
+        maxlev = std::max<int32_t>(maxlev, static_cast<int32_t>(a.levels));
+        const uint32_t nunits = unit_count(a.nb, a.U);
+        for (uint32_t u = 0; u < nunits; ++u) build.push_back(make_uint2(i, u));
+        for (uint32_t k = 1; k < a.levels; ++k) {
+            const uint32_t cnt = a.nb - (1u << k) + 1;
+            for (uint32_t j = 0; j < cnt; j += kLevelChunk)
+                lvl[k].push_back(make_uint4(i, k, j, std::min(kLevelChunk, cnt - j)));
+        }
+        for (int64_t j = 0; j < qc; j += kQueryChunk)
+            b->h_qitems.push_back(make_uint4(i, static_cast<uint32_t>(j),
+                                             static_cast<uint32_t>(std::min<int64_t>(kQueryChunk, qc - j)), 0));
+    }
+    if (b->limit > 0xffffffffLL * 4) {
+        delete b;
+        return set_error(RMQ_EINVAL, "rmq_batch_create: value span too large");
+    }
+    std::vector<uint4> lvl_flat;
+    BatchParams &P = b->P;
+    std::memset(&P, 0, sizeof(P));
+    P.maxlev = maxlev;
+    for (int k = 0; k <= kMaxLevels; ++k) P.lvl_start[k] = 0;
+    for (int k = 1; k < kMaxLevels; ++k) {
+        P.lvl_start[k] = static_cast<int32_t>(lvl_flat.size());
+        lvl_flat.insert(lvl_flat.end(), lvl[k].begin(), lvl[k].end());
+    }
+    P.lvl_start[kMaxLevels] = static_cast<int32_t>(lvl_flat.size());
+    for (int k = maxlev; k < kMaxLevels; ++k) P.lvl_start[k] = P.lvl_start[kMaxLevels];
+    P.nbuild = static_cast<int32_t>(build.size());
+    P.nqitems = static_cast<int32_t>(b->h_qitems.size());
+
+    // one allocation: arrays | build | lvl | qitems | counter | workspace
+    const size_t o_arr = 0;
+    const size_t o_build = align_up(o_arr + sizeof(BatchArray) * narrays, 256);
+    const size_t o_lvl = align_up(o_build + sizeof(uint2) * build.size(), 256);
+    const size_t o_q = align_up(o_lvl + sizeof(uint4) * lvl_flat.size(), 256);
+    const size_t o_cnt = align_up(o_q + sizeof(uint4) * b->h_qitems.size(), 256);
+    const size_t o_ws = align_up(o_cnt + 256, 256);
+    b->ws_bytes = sizeof(Entry) * static_cast<size_t>(ws_entries);
+    b->mem_bytes = o_ws + b->ws_bytes;
+    cudaError_t err = cudaMalloc(&b->mem, b->mem_bytes);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        size_t bytes = b->mem_bytes;
+        delete b;
+        return set_error(RMQ_ENOMEM, "rmq_batch_create: cudaMalloc(%zu bytes) failed", bytes);
+    }
+    char *base = static_cast<char *>(b->mem);
+    err = cudaMemcpy(base + o_arr, b->h_arrays.data(), sizeof(BatchArray) * narrays,
+                     cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && !build.empty())
+        err = cudaMemcpy(base + o_build, build.data(), sizeof(uint2) * build.size(),
+                         cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && !lvl_flat.empty())
+        err = cudaMemcpy(base + o_lvl, lvl_flat.data(), sizeof(uint4) * lvl_flat.size(),
+                         cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && !b->h_qitems.empty())
+        err = cudaMemcpy(base + o_q, b->h_qitems.data(), sizeof(uint4) * b->h_qitems.size(),
+                         cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemset(base + o_cnt, 0, 256);
+    if (err != cudaSuccess) {
+        rc = cuda_fail(err, "rmq_batch_create: upload");
+        cudaFree(b->mem);
+        delete b;
+        return rc;
+    }
+    P.arrays = reinterpret_cast<const BatchArray *>(base + o_arr);
+    P.build = reinterpret_cast<const uint2 *>(base + o_build);
+    P.lvl = reinterpret_cast<const uint4 *>(base + o_lvl);
+    P.qitems = reinterpret_cast<const uint4 *>(base + o_q);
+    P.invalid = reinterpret_cast<unsigned long long *>(base + o_cnt);
+    P.ws = reinterpret_cast<Entry *>(base + o_ws);
+    P.limit = b->limit;
+    *out = b;
+    return RMQ_OK;
+}
+
+static int batch_args(const rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
+                      float *d_val, int32_t *d_idx, const char *who) {
+    if (!b) return set_error(RMQ_EINVAL, "%s: batch is NULL", who);
+    if (!d_vals || reinterpret_cast<uintptr_t>(d_vals) % 4)
+        return set_error(RMQ_EINVAL, "%s: d_vals NULL or not 4-byte aligned", who);
+    if (b->total_q > 0 && (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8))
+        return set_error(RMQ_EINVAL, "%s: d_queries NULL or not 8-byte aligned", who);
+    if (b->total_q > 0 && !d_val && !d_idx)
+        return set_error(RMQ_EINVAL, "%s: both outputs are NULL", who);
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return cuda_fail(err, who);
+    if (dev != b->device)
+        return set_error(RMQ_EINVAL, "%s: batch planned on device %d, current is %d", who,
+                         b->device, dev);
+    return RMQ_OK;
+}
+
+int rmq_batch_run(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries, float *d_val,
+                  int32_t *d_idx, rmq_stream_t stream) {
+    int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_run");
+    if (rc) return rc;
+    DeviceInfo dev;
+    rc = device_info(&dev);
+    if (rc) return rc;
+    BatchParams P = b->P;
+    P.A = d_vals;
+    P.Q = reinterpret_cast<const int2 *>(d_queries);
+    P.val = d_val;
+    P.idx = d_idx;
+    const bool aligned = reinterpret_cast<uintptr_t>(d_vals) % 16 == 0;
+    void *kern = aligned ? reinterpret_cast<void *>(batch_kernel<true>)
+                         : reinterpret_cast<void *>(batch_kernel<false>);
+    int &per_sm = g_batch_per_sm[aligned ? 1 : 0];
+    cudaError_t err = cudaSuccess;
+    if (per_sm == 0) {
+        err = aligned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<true>,
+                                                                      kThreads, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<false>,
+                                                                      kThreads, 0);
+        if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run: occupancy");
+        if (per_sm < 1) return set_error(RMQ_ENOTSUP, "rmq_batch_run: kernel cannot be resident");
+    }
+    const unsigned grid = static_cast<unsigned>(dev.sms * per_sm);
+    void *args[] = {&P};
+    err = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run: cooperative launch");
+    return RMQ_OK;
+}
+
+int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
+                            float *d_val, int32_t *d_idx, rmq_stream_t stream) {
+    int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_run_per_array");
+    if (rc) return rc;
+    DeviceInfo dev;
+    rc = device_info(&dev);
+    if (rc) return rc;
+    Entry *ws = b->P.ws;
+    std::vector<int64_t> qcount(b->narrays, 0);
+    for (const uint4 &w : b->h_qitems) qcount[w.x] += w.z;
+    for (int32_t i = 0; i < b->narrays; ++i) {
+        const BatchArray &a = b->h_arrays[i];
+        BuildPlan p;
+        p.A = d_vals + a.off;
+        p.n = a.n;
+        p.bs = a.bs;
+        p.nb = a.nb;
+        p.levels = a.levels;
+        p.aligned = reinterpret_cast<uintptr_t>(p.A) % 16 == 0;
+        p.pre = ws + a.pre;
+        p.suf = ws + a.pre + a.n;
+        p.st = ws + a.st;
+        cudaError_t err = launch_build(p, dev, stream);
+        if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run_per_array: build");
+        if (qcount[i] == 0) continue;
+        QueryArgs q;
+        q.Q = reinterpret_cast<const int2 *>(d_queries) + a.qoff;
+        q.q = qcount[i];
+        q.val = d_val ? d_val + a.qoff : nullptr;
+        q.idx = d_idx ? d_idx + a.qoff : nullptr;
+        q.invalid = b->P.invalid;
+        err = launch_query(p, q, dev, stream);
+        if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run_per_array: query");
+    }
+    return RMQ_OK;
+}
+
+int rmq_batch_scatter_grad(const rmq_batch_t *b, const int32_t *d_idx, const float *d_grad_out,
+                           float *d_grad_vals, int32_t accumulate, rmq_stream_t stream) {
+    if (!b || !d_idx || !d_grad_out || !d_grad_vals)
+        return set_error(RMQ_EINVAL, "rmq_batch_scatter_grad: NULL argument");
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    cudaError_t err = cudaSuccess;
+    if (!accumulate)
+        err = cudaMemsetAsync(d_grad_vals, 0, sizeof(float) * static_cast<size_t>(b->limit), stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_scatter_grad: memset");
+    if (b->P.nqitems > 0) {
+        unsigned grid = static_cast<unsigned>(std::min<int64_t>(b->P.nqitems, dev.sms * 8));
+        scatter_grad_kernel<<<grid, kThreads, 0, stream>>>(b->P.arrays, b->P.qitems, b->P.nqitems,
+                                                           d_idx, d_grad_out, d_grad_vals);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_scatter_grad: launch");
+    }
+    return RMQ_OK;
+}
+
+int rmq_batch_info(const rmq_batch_t *b, rmq_batch_info_t *info) {
+    if (!b || !info) return set_error(RMQ_EINVAL, "rmq_batch_info: NULL argument");
+    info->narrays = b->narrays;
+    info->values_span = b->limit;
+    info->queries_span = b->total_q;
+    info->workspace_bytes = static_cast<int64_t>(b->ws_bytes);
+    info->device_bytes = static_cast<int64_t>(b->mem_bytes);
+    info->build_items = b->P.nbuild;
+    info->query_items = b->P.nqitems;
+    info->max_levels = b->P.maxlev;
+    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) info->bucket_bs[i] = b->bucket_bs[i];
+    return RMQ_OK;
+}
+
+int rmq_batch_invalid_count(const rmq_batch_t *b, rmq_stream_t stream, int64_t *count) {
+    if (!b || !count) return set_error(RMQ_EINVAL, "rmq_batch_invalid_count: NULL argument");
+    unsigned long long v = 0;
+    cudaError_t err = cudaMemcpyAsync(&v, b->P.invalid, sizeof(v), cudaMemcpyDeviceToHost, stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_invalid_count");
+    *count = static_cast<int64_t>(v);
+    return RMQ_OK;
+}
+
+int rmq_batch_free(rmq_batch_t *b) {
+    if (!b) return RMQ_OK;
+    cudaError_t err = cudaFree(b->mem);
+    delete b;
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_free");
+    return RMQ_OK;
+}
+
+int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
+                       const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
+                       const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
+                       rmq_stream_t stream, int32_t *h_bucket_bs) {
+    if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts || !h_bucket_bs)
+        return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
+    if (reps < 1) reps = 1;
+    std::vector<std::vector<int32_t>> members(RMQ_BATCH_BUCKETS);
+    for (int32_t i = 0; i < narrays; ++i) {
+        if (h_lengths[i] <= 0) return set_error(RMQ_EINVAL, "rmq_batch_autotune: empty array %d", i);
+        members[bucket_of(h_lengths[i])].push_back(i);
+    }
+    static const int32_t cands[] = {64, 256, 1024, 4096, 16384, 65536};
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_autotune: events");
+    int rc = RMQ_OK;
+    for (int bk = 0; bk < RMQ_BATCH_BUCKETS && rc == RMQ_OK; ++bk) {
+        h_bucket_bs[bk] = 0;
+        const std::vector<int32_t> &m = members[bk];
+        if (m.empty()) continue;
+        std::vector<int64_t> s, l, qs, qc;
+        for (int32_t i : m) {
+            s.push_back(h_starts[i]);
+            l.push_back(h_lengths[i]);
+            qs.push_back(h_qstarts[i]);
+            qc.push_back(h_qcounts[i]);
+        }
+        const int64_t maxlen = int64_t(2) << bk;
+        float best_ms = 0.f;
+        for (int32_t c : cands) {
+            if (c > 2 * maxlen && h_bucket_bs[bk] != 0) break;
+            int32_t cfg[RMQ_BATCH_BUCKETS] = {0};
+            cfg[bk] = c;
+            rmq_batch_t *sub = nullptr;
+            rc = rmq_batch_create(static_cast<int32_t>(m.size()), s.data(), l.data(), qs.data(),
+                                  qc.data(), cfg, &sub);
+            if (rc) break;
+            rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);  // warm
+            if (!rc) {
+                cudaEventRecord(e0, stream);
+                for (int r = 0; r < reps && !rc; ++r)
+                    rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);
+                cudaEventRecord(e1, stream);
+                err = cudaEventSynchronize(e1);
+                if (err != cudaSuccess && !rc) rc = cuda_fail(err, "rmq_batch_autotune: timing");
+            }
+            float ms = 0.f;
+            if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+            rmq_batch_free(sub);
+            if (rc) break;
+            if (h_bucket_bs[bk] == 0 || ms < best_ms) {
+                best_ms = ms;
+                h_bucket_bs[bk] = c;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+}  // extern "C"

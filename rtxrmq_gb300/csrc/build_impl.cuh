@@ -1,0 +1,236 @@
+// build_impl.cuh -- the CTA-level unit builder shared by the plain build
+// kernel (build.cu) and the persistent batch kernel (batch.cu).
+//
+// For one array A[0..n) cut into blocks of bs it produces
+//   pre[i]  = leftmost minimum of A[blockstart(i) .. i]
+//   suf[i]  = leftmost minimum of A[i .. blockend(i)]
+//   bmin[b] = leftmost minimum of block b
+// which replace the reference's per-element triangles and per-block minimum
+// triangles (src/device_tools.cuh:139-169, kernel_min_blocks 243-253,
+// compute_min_blocks src/rtx.h:3-22).
+//
+// One CTA owns a "unit": one block when blocks are large, or G whole blocks
+// (G * bs <= 4096 elements) when they are small. A unit is streamed in
+// 4096-element tiles (16 consecutive floats per thread, float4 loads aligned
+// on absolute element indices): suffix pass right-to-left, then prefix pass
+// left-to-right (re-reading lines the suffix pass just brought into L2), each
+// tile a thread-local scan plus a CTA-wide scan, carried across tiles.
+// Results are staged in shared memory and written with coalesced stores.
+//
+// Segmented scans without flags: every element becomes one 64-bit composite
+//   [segment rank | fkey(value) | local index | -0.0 bit]
+// whose unsigned minimum is the leftmost minimum. In the prefix direction
+// earlier blocks of the unit get a larger rank, in the suffix direction later
+// blocks do, so one min-scan over the unit restarts at every block boundary.
+#pragma once
+
+#include "common.cuh"
+
+namespace rmq {
+
+constexpr int kBuildThreads = 256;
+constexpr int kBuildEPT = 16;                           // elements per thread per tile
+constexpr int kBuildTile = kBuildThreads * kBuildEPT;   // 4096
+constexpr int kBuildWarps = kBuildThreads / 32;
+constexpr uint32_t kUnitTarget = 4096;                  // elements per multi-block unit
+constexpr int kStageEntries = kBuildTile + kBuildTile / 16;
+
+struct UnitLayout {
+    uint32_t G;           // blocks per unit
+    uint32_t key_shift;   // 32 when G == 1, else 17
+    uint32_t seg_shift;   // 49 when G > 1 (63, unused, otherwise)
+    uint32_t local_mask;  // 0x7fffffff when G == 1, else 0xffff
+};
+
+inline UnitLayout make_unit_layout(uint32_t bs, uint32_t nb) {
+    UnitLayout U;
+    U.G = (bs >= kUnitTarget) ? 1u : (kUnitTarget / bs);
+    if (U.G > nb) U.G = nb;
+    if (U.G <= 1) {
+        U.G = 1;
+        U.key_shift = 32;
+        U.seg_shift = 63;
+        U.local_mask = 0x7fffffffu;
+    } else {
+        U.key_shift = 17;
+        U.seg_shift = 49;
+        U.local_mask = 0xffffu;
+    }
+    return U;
+}
+
+inline uint32_t unit_count(uint32_t nb, const UnitLayout &U) { return (nb + U.G - 1) / U.G; }
+
+// One array to build: A is the base of the value buffer, the array occupies
+// A[off .. off + n); loads never go past A[limit - 1].
+struct UnitJob {
+    const float *A;
+    int64_t off;
+    int64_t limit;
+    uint32_t n;
+    uint32_t bs;
+    UnitLayout U;
+    Div31 dv;
+    Entry *pre;   // [n], array-relative
+    Entry *suf;   // [n]
+    Entry *bmin;  // [nb]
+};
+
+__device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return b < a ? b : a; }
+
+__device__ __forceinline__ uint64_t unit_comp(uint32_t bits, uint32_t local, uint32_t segf,
+                                              const UnitLayout &U) {
+    const uint64_t nz = (bits == 0x80000000u) ? 1ull : 0ull;
+    return (static_cast<uint64_t>(segf) << U.seg_shift) |
+           (static_cast<uint64_t>(fkey(bits)) << U.key_shift) |
+           (static_cast<uint64_t>(local) << 1) | nz;
+}
+
+__device__ __forceinline__ Entry unit_decode(uint64_t c, uint32_t ustart, const UnitLayout &U) {
+    Entry e;
+    const uint32_t key = static_cast<uint32_t>(c >> U.key_shift);
+    e.bits = funkey(key, static_cast<uint32_t>(c & 1ull));
+    e.idx = ustart + (static_cast<uint32_t>(c >> 1) & U.local_mask);
+    return e;
+}
+
+// Exclusive min-scan of one value per thread across the CTA, in thread order
+// (REV = false) or reverse thread order (REV = true); `total` receives the
+// CTA-wide minimum.
+template <bool REV>
+__device__ __forceinline__ uint64_t cta_exclusive_min(uint64_t v, uint64_t *s_warp,
+                                                      uint64_t &total) {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    uint64_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t t = REV ? __shfl_down_sync(0xffffffffu, inc, o)
+                               : __shfl_up_sync(0xffffffffu, inc, o);
+        const bool ok = REV ? (lane + o < 32) : (lane >= o);
+        if (ok) inc = umin64(inc, t);
+    }
+    uint64_t ex = REV ? __shfl_down_sync(0xffffffffu, inc, 1)
+                      : __shfl_up_sync(0xffffffffu, inc, 1);
+    if (REV ? (lane == 31) : (lane == 0)) ex = ~0ull;
+    if (REV ? (lane == 0) : (lane == 31)) s_warp[warp] = inc;
+    __syncthreads();
+    uint64_t wex = ~0ull, tot = ~0ull;
+#pragma unroll
+    for (int w = 0; w < kBuildWarps; ++w) {
+        const uint64_t s = s_warp[w];
+        tot = umin64(tot, s);
+        if (REV ? (w > warp) : (w < warp)) wex = umin64(wex, s);
+    }
+    total = tot;
+    __syncthreads();
+    return umin64(ex, wex);
+}
+
+// Build unit `u` of job J with the whole CTA (kBuildThreads threads).
+// stage: kStageEntries entries of shared memory; s_warp: kBuildWarps words.
+template <bool ALIGNED>
+__device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *stage,
+                                           uint64_t *s_warp) {
+    const UnitLayout U = J.U;
+    const uint32_t ustart = u * U.G * J.bs;
+    const uint32_t uend = min(ustart + U.G * J.bs, J.n);
+    const int64_t a_lo = J.off + ustart;        // absolute [a_lo, a_hi)
+    const int64_t a_hi = J.off + uend;
+    const int64_t t_first = ALIGNED ? (a_lo & ~int64_t(3)) : a_lo;
+    const uint32_t ntiles = static_cast<uint32_t>((a_hi - t_first + kBuildTile - 1) / kBuildTile);
+
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool suffix = (pass == 0);
+        uint64_t carry = ~0ull;
+#pragma unroll 1
+        for (uint32_t tt = 0; tt < ntiles; ++tt) {
+            const uint32_t t = suffix ? (ntiles - 1 - tt) : tt;
+            const int64_t t0 = t_first + static_cast<int64_t>(t) * kBuildTile;
+            const int64_t base = t0 + static_cast<int64_t>(threadIdx.x) * kBuildEPT;
+
+            uint32_t bits[kBuildEPT];
+            if (ALIGNED && base + kBuildEPT <= J.limit) {
+                const float4 *src = reinterpret_cast<const float4 *>(J.A + base);
+#pragma unroll
+                for (int v = 0; v < kBuildEPT / 4; ++v) {
+                    const float4 f = __ldg(src + v);
+                    bits[4 * v + 0] = __float_as_uint(f.x);
+                    bits[4 * v + 1] = __float_as_uint(f.y);
+                    bits[4 * v + 2] = __float_as_uint(f.z);
+                    bits[4 * v + 3] = __float_as_uint(f.w);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < kBuildEPT; ++j) {
+                    const int64_t g = base + j;
+                    bits[j] = (g >= a_lo && g < a_hi) ? __float_as_uint(__ldg(J.A + g)) : 0u;
+                }
+            }
+
+            uint64_t c[kBuildEPT];
+#pragma unroll
+            for (int j = 0; j < kBuildEPT; ++j) {
+                const int64_t g = base + j;
+                if (g >= a_lo && g < a_hi) {
+                    const uint32_t local = static_cast<uint32_t>(g - a_lo);
+                    uint32_t segf = 0;
+                    if (U.G > 1) {
+                        const uint32_t seg = div31(local, J.dv);
+                        segf = suffix ? seg : (U.G - 1 - seg);
+                    }
+                    c[j] = unit_comp(bits[j], local, segf, U);
+                } else {
+                    c[j] = ~0ull;
+                }
+            }
+            uint64_t agg;
+            if (suffix) {
+#pragma unroll
+                for (int j = kBuildEPT - 2; j >= 0; --j) c[j] = umin64(c[j], c[j + 1]);
+                agg = c[0];
+            } else {
+#pragma unroll
+                for (int j = 1; j < kBuildEPT; ++j) c[j] = umin64(c[j], c[j - 1]);
+                agg = c[kBuildEPT - 1];
+            }
+            uint64_t total;
+            uint64_t ex = suffix ? cta_exclusive_min<true>(agg, s_warp, total)
+                                 : cta_exclusive_min<false>(agg, s_warp, total);
+            ex = umin64(ex, carry);
+            carry = umin64(carry, total);
+
+#pragma unroll
+            for (int j = 0; j < kBuildEPT; ++j)
+                stage[threadIdx.x * (kBuildEPT + 1) + j] = unit_decode(umin64(c[j], ex), ustart, U);
+            __syncthreads();
+
+            Entry *out = suffix ? J.suf : J.pre;
+#pragma unroll 4
+            for (int k = 0; k < kBuildEPT; ++k) {
+                const uint32_t e = threadIdx.x + k * kBuildThreads;
+                const int64_t g = t0 + e;
+                if (g >= a_lo && g < a_hi) {
+                    const Entry en = stage[e + (e >> 4)];
+                    const uint32_t local = static_cast<uint32_t>(g - J.off);
+                    __stcs(reinterpret_cast<uint2 *>(out + local), make_uint2(en.bits, en.idx));
+                    if (!suffix) {
+                        // block minimum = prefix minimum at the block's last element
+                        const uint32_t ul = local - ustart;
+                        bool last = (g + 1 == a_hi);
+                        uint32_t seg = 0;
+                        if (U.G > 1) {
+                            seg = div31(ul, J.dv);
+                            last = last || (ul + 1 == (seg + 1) * J.bs);
+                        }
+                        if (last) J.bmin[u * U.G + seg] = en;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace rmq

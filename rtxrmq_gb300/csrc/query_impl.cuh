@@ -1,0 +1,182 @@
+// query_impl.cuh -- the CTA-level query body shared by the plain query kernel
+// (query.cu) and the persistent batch kernel (batch.cu).
+//
+// It replaces RTX_blocks' ray programs (src/rtx_kernels.cu:85-193 for
+// values, 350-465 for indices). The reference fires up to three rays per
+// query: one through the fully covered blocks lB+1..rB-1, one through the
+// left partial block and one through the right partial block, and keeps the
+// closest hit. Here the same decomposition is answered from arrays:
+//   left partial block   -> suf[l]
+//   right partial block  -> pre[r]
+//   full blocks between  -> two sparse-table entries (L2-resident)
+// A query inside one block (the reference's single-ray case,
+// src/rtx_kernels.cu:116-135) is answered from pre/suf when it touches a
+// block edge, otherwise by a warp-cooperative scan of A[l..r] that reduces
+// order-preserving keys with __reduce_min_sync.
+//
+// Differences from the reference kept on purpose: ties between rays are
+// resolved leftmost (the reference compares rays with strict `<` in the
+// order middle, left, right, src/rtx_kernels.cu:451-465), values are the
+// exact bits of A[idx] (the reference returns payload + min, rtx.h:109,
+// rtx_kernels.cu:179), and a miss cannot overwrite a minimum
+// (src/rtx_kernels.cu:80-83).
+#pragma once
+
+#include "common.cuh"
+
+namespace rmq {
+
+// One built array: values A[off .. off + n) of the buffer A (loads never go
+// past A[limit - 1]); structure arrays are array-relative.
+struct V1View {
+    const float *A;
+    int64_t off;
+    int64_t limit;
+    uint32_t n;
+    uint32_t bs;
+    uint32_t nb;
+    Div31 dv;
+    const Entry *pre;
+    const Entry *suf;
+    const Entry *st;
+};
+
+struct QueryOut {
+    const int2 *Q;        // queries of this array (local l, r)
+    float *val;           // outputs aligned with Q, may be null
+    int32_t *idx;         // may be null
+    unsigned long long *invalid;
+};
+
+__device__ __forceinline__ void put_result(const QueryOut &o, int64_t i, Entry e) {
+    if (o.val) __stcs(o.val + i, __uint_as_float(e.bits));
+    if (o.idx) __stcs(o.idx + i, static_cast<int32_t>(e.idx));
+}
+
+__device__ __forceinline__ void put_invalid(const QueryOut &o, int64_t i) {
+    if (o.val) __stcs(o.val + i, __uint_as_float(0x7fc00000u));
+    if (o.idx) __stcs(o.idx + i, -1);
+    if (o.invalid) atomicAdd(o.invalid, 1ull);
+}
+
+// Leftmost minimum of local A[l..r] computed by the whole warp. All 32 lanes
+// call it with the same (l, r); every lane gets the result. ALIGNED: the
+// buffer base is 16-byte aligned, so float4 loads on absolute indices are.
+template <bool ALIGNED>
+__device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, uint32_t r,
+                                                 int lane) {
+    uint64_t best = ~0ull;
+    const int64_t al = v.off + l, ar = v.off + r;
+    if (ALIGNED) {
+        for (int64_t p = (al & ~int64_t(3)) + 4 * lane; p <= ar; p += 128) {
+            uint32_t b[4];
+            if (p + 3 < v.limit) {
+                const float4 f = __ldg(reinterpret_cast<const float4 *>(v.A + p));
+                b[0] = __float_as_uint(f.x);
+                b[1] = __float_as_uint(f.y);
+                b[2] = __float_as_uint(f.z);
+                b[3] = __float_as_uint(f.w);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    b[c] = (p + c <= ar) ? __float_as_uint(__ldg(v.A + p + c)) : 0u;
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int64_t g = p + c;
+                if (g >= al && g <= ar) {
+                    const uint64_t k = (static_cast<uint64_t>(fkey(b[c])) << 32) |
+                                       static_cast<uint32_t>(g - v.off);
+                    best = k < best ? k : best;
+                }
+            }
+        }
+    } else {
+        for (int64_t g = al + lane; g <= ar; g += 32) {
+            const uint64_t k = (static_cast<uint64_t>(fkey(__float_as_uint(__ldg(v.A + g)))) << 32) |
+                               static_cast<uint32_t>(g - v.off);
+            best = k < best ? k : best;
+        }
+    }
+    const uint32_t key = static_cast<uint32_t>(best >> 32);
+    const uint32_t kmin = __reduce_min_sync(0xffffffffu, key);
+    const uint32_t cand = (key == kmin) ? static_cast<uint32_t>(best) : 0xffffffffu;
+    Entry e;
+    e.idx = __reduce_min_sync(0xffffffffu, cand);
+    e.bits = __float_as_uint(__ldg(v.A + v.off + e.idx));
+    return e;
+}
+
+// Answer queries [q0, q1) of one array with the whole CTA. The loop is
+// uniform across the CTA (warp-cooperative scans need full warps).
+// QPT queries per thread per iteration keep several independent lookups in
+// flight per thread.
+template <bool ALIGNED, int QPT>
+__device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o, int64_t q0,
+                                             int64_t q1) {
+    const int lane = threadIdx.x & 31;
+    const int64_t step = static_cast<int64_t>(blockDim.x) * QPT;
+    for (int64_t base = q0; base < q1; base += step) {
+        uint32_t l[QPT], r[QPT];
+        bool act[QPT], ok[QPT], scan[QPT];
+        Entry es[QPT], ep[QPT], ea[QPT], eb[QPT];
+#pragma unroll
+        for (int k = 0; k < QPT; ++k) {
+            const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
+            act[k] = i < q1;
+            int2 qq = make_int2(0, 0);
+            if (act[k]) qq = __ldcs(o.Q + i);
+            ok[k] = act[k] && qq.x >= 0 && qq.x <= qq.y && static_cast<uint32_t>(qq.y) < v.n;
+            l[k] = ok[k] ? static_cast<uint32_t>(qq.x) : 0u;
+            r[k] = ok[k] ? static_cast<uint32_t>(qq.y) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < QPT; ++k) {
+            const uint32_t lB = div31(l[k], v.dv);
+            const uint32_t rB = div31(r[k], v.dv);
+            const bool cross = ok[k] && lB != rB;
+            const uint32_t bstart = lB * v.bs;
+            const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
+            const bool same = ok[k] && lB == rB;
+            const bool use_suf = cross || (same && r[k] == bend);
+            const bool use_pre = cross || (same && l[k] == bstart);
+            scan[k] = same && !use_suf && !use_pre;
+            es[k] = use_suf ? v.suf[l[k]] : entry_max();
+            ep[k] = use_pre ? v.pre[r[k]] : entry_max();
+            ea[k] = entry_max();
+            eb[k] = entry_max();
+            if (cross && rB - lB >= 2u) {
+                const uint32_t lo = lB + 1u, hi = rB - 1u;
+                const int lev = ilog2(hi - lo + 1u);
+                const Entry *lvl = v.st + static_cast<size_t>(lev) * v.nb;
+                ea[k] = lvl[lo];
+                eb[k] = lvl[hi + 1u - (1u << lev)];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < QPT; ++k) {
+            if (act[k] && !scan[k]) {
+                const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
+                if (ok[k])
+                    put_result(o, i, better(better(es[k], ep[k]), better(ea[k], eb[k])));
+                else
+                    put_invalid(o, i);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < QPT; ++k) {
+            unsigned mask = __ballot_sync(0xffffffffu, scan[k]);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1u;
+                const uint32_t ls = __shfl_sync(0xffffffffu, l[k], src);
+                const uint32_t rs = __shfl_sync(0xffffffffu, r[k], src);
+                const Entry e = warp_scan_range<ALIGNED>(v, ls, rs, lane);
+                if (lane == src)
+                    put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e);
+            }
+        }
+    }
+}
+
+}  // namespace rmq

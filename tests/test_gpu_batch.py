@@ -1,0 +1,166 @@
+"""GPU: the batched ragged form (one persistent cooperative launch) against
+the CPU oracle per array, against the per-array plain path, under CUDA-graph
+capture, and the autotuner."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(x):
+    return np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+
+
+def small_ragged(seed, ties=False, align=1):
+    """~150 arrays, lengths 1 .. 2^17 (all size buckets up to 16), starts with
+    gaps and odd offsets, queries of every length class."""
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(seed)
+    lengths = np.concatenate([[1, 2, 3, 5, 31, 32, 33, 4095, 4096, 4097],
+                              np.round(2.0 ** rng.uniform(4, 17, 140))]).astype(np.int64)
+    gaps = rng.integers(0, 7, len(lengths)) * align
+    padded = (lengths + align - 1) // align * align
+    starts = np.cumsum(np.concatenate([[gaps[0]], padded[:-1] + gaps[1:]])).astype(np.int64)
+    span = int(starts[-1] + lengths[-1] + 5)
+    A = R.gen_values_int(span, 64, seed) if ties else R.gen_values_uniform(span, seed)
+    qcounts = np.maximum(1, lengths // 16).astype(np.int64)
+    qcounts[3] = 0  # an array without queries
+    qgap = rng.integers(0, 3, len(lengths))
+    qstarts = np.cumsum(np.concatenate([[0], qcounts[:-1] + qgap[1:]])).astype(np.int64)
+    Q = np.zeros((int(qstarts[-1] + qcounts[-1] + 2), 2), dtype=np.int32)
+    for i, (n, c, s) in enumerate(zip(lengths, qcounts, qstarts)):
+        if not c:
+            continue
+        mode = i % 4
+        if mode == 0:
+            q = R.gen_queries(int(c), int(n), -1, seed + i)
+        elif mode == 1:
+            q = R.gen_queries_lognormal(int(c), int(n), 0.5 * np.log(n), 0.4, seed + i)
+        elif mode == 2:
+            q = R.gen_queries(int(c), int(n), 1, seed + i)
+        else:
+            q = R.gen_queries(int(c), int(n), int(min(n, 33)), seed + i)
+        Q[s:s + c] = q
+    return starts, lengths, qstarts, qcounts, A, Q
+
+
+def expected(oracle_lib, starts, lengths, qstarts, qcounts, A, Q):
+    ev = np.full(len(Q), np.nan, np.float32)
+    ei = np.full(len(Q), -2, np.int32)
+    for s, n, qs, qc in zip(starts, lengths, qstarts, qcounts):
+        if qc:
+            a = A[s:s + n]
+            q = Q[qs:qs + qc]
+            ev[qs:qs + qc] = oracle_lib.base_val(a, q)
+            ei[qs:qs + qc] = oracle_lib.base_idx(a, q)
+    return ev, ei
+
+
+def owned_mask(qstarts, qcounts, total):
+    m = np.zeros(total, bool)
+    for s, c in zip(qstarts, qcounts):
+        m[s:s + c] = True
+    return m
+
+
+@pytest.mark.parametrize("seed,ties,align", [(1, False, 1), (2, True, 1), (3, False, 4), (4, True, 4)])
+@pytest.mark.parametrize("cfg", ["default", "small", "large", "mixed"])
+def test_batch_matches_oracle(cuda, native, oracle_lib, seed, ties, align, cfg):
+    import torch
+
+    from rtxrmq_gb300.batch import RMQBatch
+    starts, lengths, qstarts, qcounts, A, Q = small_ragged(seed, ties, align)
+    bucket_bs = {"default": None, "small": [64] * 32, "large": [65536] * 32,
+                 "mixed": [64, 1, 7, 16, 100, 256, 1000, 4096] * 4}[cfg]
+    ev, ei = expected(oracle_lib, starts, lengths, qstarts, qcounts, A, Q)
+    own = owned_mask(qstarts, qcounts, len(Q))
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    with RMQBatch(starts, lengths, qstarts, qcounts, bucket_bs) as b:
+        v, i = b.run(dA, dQ)
+        v2, i2 = b.run_per_array(dA, dQ)
+        torch.cuda.synchronize()
+        v, i, v2, i2 = (x.cpu().numpy() for x in (v, i, v2, i2))
+        assert b.invalid_count() == 0
+    np.testing.assert_array_equal(i[own], ei[own])
+    np.testing.assert_array_equal(bits(v[own]), bits(ev[own]))
+    np.testing.assert_array_equal(i2[own], ei[own])
+    np.testing.assert_array_equal(bits(v2[own]), bits(ev[own]))
+
+
+def test_batch_invalid_and_repeat(cuda, native, oracle_lib):
+    """Invalid queries inside a batch give -1 / NaN and are counted; a plan
+    runs repeatedly on new values without re-planning."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    from rtxrmq_gb300.batch import RMQBatch
+    starts = np.array([0, 100, 300], np.int64)
+    lengths = np.array([100, 200, 50], np.int64)
+    qstarts = np.array([0, 3, 6], np.int64)
+    qcounts = np.array([3, 3, 2], np.int64)
+    Q = np.array([[0, 99], [5, 4], [0, 100], [0, 199], [10, 10], [-1, 0], [0, 49], [49, 50]], np.int32)
+    with RMQBatch(starts, lengths, qstarts, qcounts) as b:
+        for seed in range(3):
+            A = R.gen_values_uniform(350, seed)
+            v, i = b.run(torch.from_numpy(A).to(cuda), torch.from_numpy(Q).to(cuda))
+            i = i.cpu().numpy()
+            assert list(i) == [int(np.argmin(A[:100])), -1, -1, int(np.argmin(A[100:300])), 10, -1,
+                               int(np.argmin(A[300:350])), -1]
+        assert b.invalid_count() == 12
+
+
+def test_batch_graph_capture(cuda, native, oracle_lib):
+    """rmq_batch_run captured once in a CUDA graph and replayed on new data."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    from rtxrmq_gb300.batch import RMQBatch
+    starts, lengths, qstarts, qcounts, A, Q = small_ragged(7, False, 4)
+    own = owned_mask(qstarts, qcounts, len(Q))
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    outv = torch.empty(len(Q), dtype=torch.float32, device=cuda)
+    outi = torch.empty(len(Q), dtype=torch.int32, device=cuda)
+    with RMQBatch(starts, lengths, qstarts, qcounts) as b:
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            b.run(dA, dQ, outv, outi)
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            b.run(dA, dQ, outv, outi)
+        for seed in (11, 12):
+            A2 = R.gen_values_int(len(A), 1000, seed)
+            dA.copy_(torch.from_numpy(A2))
+            g.replay()
+            torch.cuda.synchronize()
+            ev, ei = expected(oracle_lib, starts, lengths, qstarts, qcounts, A2, Q)
+            np.testing.assert_array_equal(outi.cpu().numpy()[own], ei[own])
+            np.testing.assert_array_equal(bits(outv.cpu().numpy()[own]), bits(ev[own]))
+
+
+def test_autotune(cuda, native, oracle_lib, tmp_path):
+    import torch
+
+    from rtxrmq_gb300.batch import RMQBatch, autotune, bucket_of
+    starts, lengths, qstarts, qcounts, A, Q = small_ragged(5, False, 4)
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    cache = tmp_path / "tune.json"
+    cfg = autotune(starts, lengths, qstarts, qcounts, dA, dQ, reps=2, queries_host=Q, cache=cache)
+    present = set(int(b) for b in bucket_of(lengths))
+    for bk in range(32):
+        if bk in present:
+            assert cfg[bk] in (64, 256, 1024, 4096, 16384, 65536)
+        else:
+            assert cfg[bk] == 0
+    assert cache.exists()
+    assert autotune(starts, lengths, qstarts, qcounts, dA, dQ, queries_host=Q, cache=cache) == cfg
+    ev, ei = expected(oracle_lib, starts, lengths, qstarts, qcounts, A, Q)
+    own = owned_mask(qstarts, qcounts, len(Q))
+    with RMQBatch(starts, lengths, qstarts, qcounts, cfg) as b:
+        assert b.info()["bucket_bs"][:32] == cfg
+        v, i = b.run(dA, dQ)
+        np.testing.assert_array_equal(i.cpu().numpy()[own], ei[own])

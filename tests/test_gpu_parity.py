@@ -223,3 +223,37 @@ def test_cli_check_passes(native):
                             "--seed", "1321", "--check", "--nt", "4"],
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0 and "pass" in r.stdout, r.stdout + r.stderr
+
+
+def test_query_host_buffers(cuda, native, oracle_lib):
+    """rmq_query_host: pinned host buffers are read and written in place;
+    pageable buffers are served in place where the device reads pageable
+    memory, and rejected with RMQ_EINVAL elsewhere."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n, q = 200_000, 100_000
+    A = R.gen_values_uniform(n, 12)
+    Q = R.gen_queries(q, n, -2, 12)
+    ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), 1024) as ix:
+        hQ = torch.from_numpy(Q).pin_memory()
+        hV = torch.empty(q, dtype=torch.float32).pin_memory()
+        hI = torch.empty(q, dtype=torch.int32).pin_memory()
+        ix.query_host(hQ, hV, hI)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(hI.numpy(), ei)
+        np.testing.assert_array_equal(bits(hV.numpy()), bits(ev))
+        ix.query_host(hQ, None, hI)  # index mode only
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(hI.numpy(), ei)
+        v = np.full(q, np.nan, np.float32)
+        i = np.full(q, -7, np.int32)
+        try:
+            ix.query_host(Q, v, i)
+            torch.cuda.synchronize()
+        except R.RMQError as e:
+            assert e.code == -1 and "addressable" in str(e)
+        else:
+            np.testing.assert_array_equal(i, ei)
+            np.testing.assert_array_equal(bits(v), bits(ev))

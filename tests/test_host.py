@@ -175,3 +175,19 @@ def test_cli_argument_errors(native, args, code):
     CUDA call (src/tools.h:76-95 checks)."""
     r = subprocess.run([str(CLI), *args], capture_output=True, text=True, timeout=60)
     assert r.returncode == code, r.stdout + r.stderr
+
+
+def test_ragged_workload_shapes(native):
+    from rtxrmq_gb300 import workloads as W
+    w = W.ragged(narrays=64, umin=8, umax=12, total_q=20000, seed=3)
+    assert w.lengths.min() >= 256 and w.lengths.max() <= 4096
+    assert (w.starts % 4 == 0).all() and w.total_q == 20000 == int(w.qcounts.sum())
+    assert w.span >= int((w.starts + w.lengths).max())
+    for s, c, n in zip(w.qstarts, w.qcounts, w.lengths):
+        q = w.queries[s:s + c]
+        assert (q[:, 0] >= 0).all() and (q[:, 0] <= q[:, 1]).all() and (q[:, 1] < n).all()
+    # queries proportional to length
+    assert abs(np.corrcoef(w.qcounts, w.lengths)[0, 1] - 1) < 1e-3
+    d = W.differentiable_rows(nrows=8, lmin=1000, lmax=2000, q_per_row=100, seed=4)
+    assert d.span == int(d.lengths.sum()) and (d.qcounts == 100).all()
+    assert abs(float(d.values.mean())) < 0.1
