@@ -144,13 +144,27 @@ def algorithmic_bytes(Q: np.ndarray, n: int, bs: int, out_bytes: int) -> tuple[f
     bend = np.minimum(bstart + bs, n) - 1
     edge = (~cross) & ((l == bstart) | (r == bend))
     scan = (~cross) & ~edge
-    sectors = (r * 4) // 32 - (l * 4) // 32 + 1
+
+    def sectors(a, b):  # 32-byte sectors spanned by A[a..b]
+        return (b * 4) // 32 - (a * 4) // 32 + 1
+
     per_q = 8 + out_bytes
-    total = (per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge.sum() +
-             32.0 * sectors[scan].sum())
+    total = per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge.sum()
+    micro = bs % 32 == 0 and bs >= 64
+    if micro:
+        # sub-block level: the partial 32-element micro-blocks at both ends,
+        # plus two micro-table entries when micro-blocks lie between
+        ls, rs = l[scan], r[scan]
+        ml, mr = ls // 32, rs // 32
+        one = ml == mr
+        sec = np.where(one, sectors(ls, rs),
+                       sectors(ls, ml * 32 + 31) + sectors(mr * 32, rs) + 2 * (mr - ml >= 2))
+    else:
+        sec = sectors(l[scan], r[scan])
+    total += 32.0 * sec.sum()
     return float(total), {"cross_block": float(cross.mean()), "edge": float(edge.mean()),
-                          "scan": float(scan.mean()),
-                          "mean_scan_sectors": float(sectors[scan].mean()) if scan.any() else 0.0}
+                          "same_block": float(scan.mean()), "sub_block_level": bool(micro),
+                          "mean_same_block_sectors": float(sec.mean()) if scan.any() else 0.0}
 
 
 def time_steps(fn, steps, warmup, stream, barrier):

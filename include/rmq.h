@@ -57,7 +57,14 @@ typedef struct rmq_info {
     int32_t aligned;      /* 1 when d_vals is 16-byte aligned           */
     int64_t table_bytes;  /* sparse table (block minima and levels)     */
     int64_t struct_bytes; /* all device memory owned by the handle      */
+    int32_t micro_levels; /* levels of the sub-block table (0 = none)   */
+    int32_t reserved;
+    int64_t micro_table_bytes;
 } rmq_info_t;
+
+/* rmq_build_ex flags */
+#define RMQ_BUILD_NO_MICRO 1u  /* no sub-block level: same-block queries are
+                                  answered by warp-cooperative scans */
 
 /*
  * Build the index over d_vals[0..n) with block size bs (bs <= 0: default).
@@ -73,6 +80,17 @@ typedef struct rmq_info {
  */
 int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
               rmq_handle_t **out);
+
+/*
+ * rmq_build with options. When bs is a multiple of 32 (and >= 64) the index
+ * also gets a sub-block level -- minima of 32-element micro-blocks and a
+ * sparse table over them, truncated to windows shorter than one block -- so
+ * that a query inside one block reads two 128-byte lines and two table
+ * entries instead of scanning A[l..r]. RMQ_BUILD_NO_MICRO leaves it out.
+ * rmq_build(...) is rmq_build_ex(..., 0, ...).
+ */
+int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags,
+                 rmq_stream_t stream, rmq_handle_t **out);
 
 /*
  * Answer q queries d_queries[2*i] = l, d_queries[2*i+1] = r.

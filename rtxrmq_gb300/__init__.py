@@ -72,15 +72,16 @@ class RMQIndex:
     index is used (the index refers to it, it does not copy it).
     """
 
-    def __init__(self, values, bs: int = 0, stream=None):
+    def __init__(self, values, bs: int = 0, stream=None, micro: bool = True):
         import torch
         if values.dtype != torch.float32 or values.dim() != 1:
             raise TypeError("values must be a 1-D float32 CUDA tensor")
         lib = load()
         self._values = values
         self._h = C.c_void_p()
-        check(lib.rmq_build(_dptr(values), values.numel(), int(bs), _stream_handle(stream),
-                            C.byref(self._h)))
+        flags = 0 if micro else 1  # RMQ_BUILD_NO_MICRO
+        check(lib.rmq_build_ex(_dptr(values), values.numel(), int(bs), flags,
+                               _stream_handle(stream), C.byref(self._h)))
 
     def info(self) -> dict:
         inf = rmq_info_t()

@@ -32,7 +32,11 @@ class RMQError(RuntimeError):
 
 class rmq_info_t(C.Structure):
     _fields_ = [("n", C.c_int64), ("bs", C.c_int64), ("nb", C.c_int64), ("levels", C.c_int32),
-                ("aligned", C.c_int32), ("table_bytes", C.c_int64), ("struct_bytes", C.c_int64)]
+                ("aligned", C.c_int32), ("table_bytes", C.c_int64), ("struct_bytes", C.c_int64),
+                ("micro_levels", C.c_int32), ("reserved", C.c_int32),
+                ("micro_table_bytes", C.c_int64)]
+
+RMQ_BUILD_NO_MICRO = 1
 
 
 RMQ_BATCH_BUCKETS = 32
@@ -50,6 +54,7 @@ _vp, _i64, _i32, _u64, _dbl = C.c_void_p, C.c_int64, C.c_int32, C.c_uint64, C.c_
 # name -> (restype, argtypes); every symbol include/rmq.h declares
 SIGNATURES = {
     "rmq_build": (C.c_int, [_vp, _i64, _i64, _vp, C.POINTER(_vp)]),
+    "rmq_build_ex": (C.c_int, [_vp, _i64, _i64, C.c_uint32, _vp, C.POINTER(_vp)]),
     "rmq_query": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "rmq_query_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "rmq_free": (C.c_int, [_vp]),

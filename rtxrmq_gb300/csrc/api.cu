@@ -89,8 +89,15 @@ int rmq_bs_from_nb(int64_t n, int64_t nb, int64_t *bs) {
 
 int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
               rmq_handle_t **out) {
+    return rmq_build_ex(d_vals, n, bs, 0, stream, out);
+}
+
+int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq_stream_t stream,
+                 rmq_handle_t **out) {
     g_err[0] = '\0';
     if (!out) return set_error(RMQ_EINVAL, "rmq_build: out is NULL");
+    if (flags & ~static_cast<uint32_t>(RMQ_BUILD_NO_MICRO))
+        return set_error(RMQ_EINVAL, "rmq_build_ex: unknown flags 0x%x", flags);
     *out = nullptr;
     if (n <= 0 || n > 0x7fffffffLL)
         return set_error(RMQ_EINVAL, "rmq_build: n=%lld outside [1, 2^31-1]", (long long)n);
@@ -111,10 +118,14 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
     p.nb = static_cast<uint32_t>((n + bs - 1) / bs);
     p.levels = st_levels(p.nb);
     p.aligned = (reinterpret_cast<uintptr_t>(d_vals) % 16) == 0;
+    p.mlevels = (flags & RMQ_BUILD_NO_MICRO) ? 0u : micro_levels(p.bs);
+    p.micro = p.mlevels > 0;
+    p.nmicro = p.micro ? static_cast<uint32_t>((n + kMicro - 1) / kMicro) : 0u;
 
     const size_t pre_b = align_up(sizeof(Entry) * static_cast<size_t>(n), 256);
     const size_t st_b = align_up(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels, 256);
-    const size_t total = 2 * pre_b + st_b + 256;
+    const size_t mst_b = align_up(sizeof(Entry) * static_cast<size_t>(p.nmicro) * p.mlevels, 256);
+    const size_t total = 2 * pre_b + st_b + mst_b + 256;
 
     rmq_handle_t *h = new (std::nothrow) rmq_handle_t;
     if (!h) return set_error(RMQ_ENOMEM, "rmq_build: host allocation failed");
@@ -131,7 +142,8 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
     p.pre = reinterpret_cast<Entry *>(base);
     p.suf = reinterpret_cast<Entry *>(base + pre_b);
     p.st = reinterpret_cast<Entry *>(base + 2 * pre_b);
-    h->invalid = reinterpret_cast<unsigned long long *>(base + 2 * pre_b + st_b);
+    p.mst = p.micro ? reinterpret_cast<Entry *>(base + 2 * pre_b + st_b) : nullptr;
+    h->invalid = reinterpret_cast<unsigned long long *>(base + 2 * pre_b + st_b + mst_b);
     h->mem_bytes = total;
     h->table_bytes = static_cast<int64_t>(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels);
     h->plan = p;
@@ -250,6 +262,10 @@ int rmq_info(const rmq_handle_t *h, rmq_info_t *info) {
     info->aligned = h->plan.aligned ? 1 : 0;
     info->table_bytes = h->table_bytes;
     info->struct_bytes = static_cast<int64_t>(h->mem_bytes);
+    info->micro_levels = static_cast<int32_t>(h->plan.mlevels);
+    info->reserved = 0;
+    info->micro_table_bytes =
+        static_cast<int64_t>(sizeof(Entry) * static_cast<size_t>(h->plan.nmicro) * h->plan.mlevels);
     return RMQ_OK;
 }
 

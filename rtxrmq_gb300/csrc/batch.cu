@@ -79,6 +79,8 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     v.pre = P.ws + a.pre;
     v.suf = P.ws + a.pre + a.n;
     v.st = P.ws + a.st;
+    v.mst = nullptr;  // batched arrays answer same-block queries with warp scans
+    v.nmicro = 0;
     return v;
 }
 
@@ -389,6 +391,10 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
         p.pre = ws + a.pre;
         p.suf = ws + a.pre + a.n;
         p.st = ws + a.st;
+        p.micro = false;
+        p.nmicro = 0;
+        p.mlevels = 0;
+        p.mst = nullptr;
         cudaError_t err = launch_build(p, dev, stream);
         if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run_per_array: build");
         if (qcount[i] == 0) continue;

@@ -34,7 +34,17 @@ struct BuildPlan {
     Entry *pre;   // [n]
     Entry *suf;   // [n]
     Entry *st;    // [levels * nb], level 0 = block minima
+    // sub-block level (only when bs is a multiple of kMicro): minima of the
+    // 32-element micro-blocks and a sparse table over them truncated to the
+    // window lengths a same-block query can need
+    bool micro;
+    uint32_t nmicro;   // ceil(n / 32)
+    uint32_t mlevels;
+    Entry *mst;        // [mlevels * nmicro]
 };
+constexpr uint32_t kMicro = 32;
+// levels of the micro table for block size bs (0 when not applicable)
+uint32_t micro_levels(uint32_t bs);
 uint32_t st_levels(uint32_t nb);
 cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s);
 

@@ -86,6 +86,8 @@ V1View view_of(const BuildPlan &p) {
     v.pre = p.pre;
     v.suf = p.suf;
     v.st = p.st;
+    v.mst = p.micro ? p.mst : nullptr;
+    v.nmicro = p.micro ? p.nmicro : 0u;
     return v;
 }
 

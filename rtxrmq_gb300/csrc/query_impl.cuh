@@ -39,7 +39,85 @@ struct V1View {
     const Entry *pre;
     const Entry *suf;
     const Entry *st;
+    // sub-block level: 32-element micro-blocks (local index / 32); null when
+    // the block size is not a multiple of 32 (same-block queries then use the
+    // warp-cooperative scan)
+    const Entry *mst;
+    uint32_t nmicro;
 };
+
+// Leftmost minimum of local A[a..b] (b - a < 32, at most 9 float4 loads)
+// computed by one thread.
+template <bool ALIGNED>
+__device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, uint32_t b) {
+    const int64_t aa = v.off + a, ab = v.off + b;
+    uint64_t best = ~0ull;
+    uint32_t best_bits = 0x7fc00000u;
+    if (ALIGNED) {
+        const int64_t p0 = aa & ~int64_t(3);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int64_t p = p0 + 4 * k;
+            if (p <= ab) {
+                uint32_t w[4];
+                if (p + 3 < v.limit) {
+                    const float4 f = __ldg(reinterpret_cast<const float4 *>(v.A + p));
+                    w[0] = __float_as_uint(f.x);
+                    w[1] = __float_as_uint(f.y);
+                    w[2] = __float_as_uint(f.z);
+                    w[3] = __float_as_uint(f.w);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+                        w[c] = (p + c <= ab) ? __float_as_uint(__ldg(v.A + p + c)) : 0u;
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int64_t g = p + c;
+                    if (g >= aa && g <= ab) {
+                        const uint64_t key = (static_cast<uint64_t>(fkey(w[c])) << 32) |
+                                             static_cast<uint32_t>(g - v.off);
+                        if (key < best) {
+                            best = key;
+                            best_bits = w[c];
+                        }
+                    }
+                }
+            }
+        }
+    } else {
+        for (int64_t g = aa; g <= ab; ++g) {
+            const uint32_t w = __float_as_uint(__ldg(v.A + g));
+            const uint64_t key = (static_cast<uint64_t>(fkey(w)) << 32) |
+                                 static_cast<uint32_t>(g - v.off);
+            if (key < best) {
+                best = key;
+                best_bits = w;
+            }
+        }
+    }
+    Entry e;
+    e.bits = best_bits;
+    e.idx = static_cast<uint32_t>(best);
+    return e;
+}
+
+// Same-block query through the sub-block level: partial micro-blocks at both
+// ends by one thread each, the micro-blocks between from the micro table.
+template <bool ALIGNED>
+__device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
+    const uint32_t ml = l >> 5, mr = r >> 5;
+    if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
+    Entry e = better(thread_range_min<ALIGNED>(v, l, ml * 32u + 31u),
+                     thread_range_min<ALIGNED>(v, mr * 32u, r));
+    if (mr - ml >= 2u) {
+        const uint32_t lo = ml + 1u, hi = mr - 1u;
+        const int k = ilog2(hi - lo + 1u);
+        const Entry *lvl = v.mst + static_cast<size_t>(k) * v.nmicro;
+        e = better(e, better(lvl[lo], lvl[hi + 1u - (1u << k)]));
+    }
+    return e;
+}
 
 struct QueryOut {
     const int2 *Q;        // queries of this array (local l, r)
@@ -162,6 +240,14 @@ __device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o,
                 else
                     put_invalid(o, i);
             }
+        }
+        if (v.mst) {
+#pragma unroll
+            for (int k = 0; k < QPT; ++k)
+                if (scan[k])
+                    put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x,
+                               micro_query<ALIGNED>(v, l[k], r[k]));
+            continue;
         }
 #pragma unroll
         for (int k = 0; k < QPT; ++k) {

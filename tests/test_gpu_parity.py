@@ -18,13 +18,17 @@ def bits(x):
     return np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
 
 
-def run_index(cuda, A, Q, bs, values=True, indices=True):
+def run_index(cuda, A, Q, bs, values=True, indices=True, micro=True):
+    """Build + query; micro=False forces the warp-scan path for queries
+    inside one block (micro=True uses the sub-block level when bs % 32 == 0)."""
     import torch
 
     import rtxrmq_gb300 as R
     dA = torch.from_numpy(np.ascontiguousarray(A, dtype=np.float32)).to(cuda)
     dQ = torch.from_numpy(np.ascontiguousarray(Q, dtype=np.int32)).to(cuda)
-    with R.RMQIndex(dA, bs) as ix:
+    with R.RMQIndex(dA, bs, micro=micro) as ix:
+        if micro and bs >= 64 and bs % 32 == 0 and bs <= len(A):
+            assert ix.info()["micro_levels"] > 0
         v, i = ix.query(dQ, values=values, indices=indices)
         torch.cuda.synchronize()
         return (None if v is None else v.cpu().numpy()), (None if i is None else i.cpu().numpy())
@@ -53,48 +57,53 @@ def all_pairs(n):
     return np.stack([l, r], axis=1).astype(np.int32)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 31, 32, 33, 127, 300])
-def test_exhaustive_small(cuda, native, oracle_lib, n):
+@pytest.mark.parametrize("micro", [True, False])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 31, 32, 33, 127, 300, 1000])
+def test_exhaustive_small(cuda, native, oracle_lib, n, micro):
     """Every (l, r) of small tie-heavy arrays, across block sizes that put
-    block edges everywhere (bs = 1 .. n)."""
+    block edges everywhere (bs = 1 .. n), with and without the sub-block level."""
     import rtxrmq_gb300 as R
     A = R.gen_values_int(n, 4, n)
     Q = all_pairs(n)
     ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
-    for bs in sorted({1, 2, 3, 4, 7, 8, 16, 31, 32, 33, 64, 100, 128, n, max(1, n // 2)}):
+    for bs in sorted({1, 2, 3, 4, 7, 8, 16, 31, 32, 33, 64, 96, 100, 128, 160, 256, 512, n,
+                      max(1, n // 2)}):
         if bs > n:
             continue
-        v, i = run_index(cuda, A, Q, bs)
+        v, i = run_index(cuda, A, Q, bs, micro=micro)
         assert_matches(A, Q, v, i, ev, ei)
 
 
+@pytest.mark.parametrize("micro", [True, False])
 @pytest.mark.parametrize("bs", [1 << 10, 1 << 12, 1 << 15, 0, 977])
-def test_config_small_range(cuda, native, oracle_lib, bs):
+def test_config_small_range(cuda, native, oracle_lib, bs, micro):
     """n=1e6 uniform values (seed 1321), q=2^20 small-range (lr=-3) queries."""
     import rtxrmq_gb300 as R
     n, q = 10**6, 1 << 20
     A = R.gen_values_uniform(n, 1321)
     Q = R.gen_queries(q, n, -3, 1321)
-    v, i = run_index(cuda, A, Q, bs)
+    v, i = run_index(cuda, A, Q, bs, micro=micro)
     assert_matches(A, Q, v, i, oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q))
 
 
+@pytest.mark.parametrize("micro", [True, False])
 @pytest.mark.parametrize("lr", [-1, -2, -3, 1, 32, 1024, 65536])
-@pytest.mark.parametrize("bs", [1 << 10, 1 << 13, 1 << 16, 12207])
-def test_length_modes_medium(cuda, native, oracle_lib, lr, bs):
+@pytest.mark.parametrize("bs", [1 << 10, 1 << 13, 1 << 16, 12207, 4000])
+def test_length_modes_medium(cuda, native, oracle_lib, lr, bs, micro):
     """n=2^22: every length mode and block-size class; oracle = the CPU
     restatement of RTX_blocks (exact, O(bs + nb) per query)."""
     import rtxrmq_gb300 as R
     n, q = 1 << 22, 1 << 16
     A = R.gen_values_uniform(n, 11)
     Q = R.gen_queries(q, n, lr, 100 + lr)
-    v, i = run_index(cuda, A, Q, bs)
+    v, i = run_index(cuda, A, Q, bs, micro=micro)
     ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
     assert_matches(A, Q, v, i, ev, ei)
 
 
-@pytest.mark.parametrize("length", [1, 32, 1 << 10, 1 << 16, 1 << 20])
-def test_tie_heavy(cuda, native, oracle_lib, length):
+@pytest.mark.parametrize("micro", [True, False])
+@pytest.mark.parametrize("length", [1, 32, 33, 1 << 10, 1 << 16, 1 << 20])
+def test_tie_heavy(cuda, native, oracle_lib, length, micro):
     """Integers in [0,256): most ranges hold many equal minima; leftmost."""
     import rtxrmq_gb300 as R
     n, q = 1 << 23, 1 << 15
@@ -102,7 +111,7 @@ def test_tie_heavy(cuda, native, oracle_lib, length):
     Q = R.gen_queries(q, n, length, 7)
     ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
     for bs in (1 << 10, 1 << 16):
-        v, i = run_index(cuda, A, Q, bs)
+        v, i = run_index(cuda, A, Q, bs, micro=micro)
         assert_matches(A, Q, v, i, ev, ei)
 
 
@@ -152,15 +161,16 @@ def test_unaligned_values(cuda, native, oracle_lib):
     Q = np.concatenate([Q, R.gen_queries(5000, n, -1, 3)])
     big = torch.from_numpy(A).to(cuda)
     for off in (1, 2, 3):
-        dA = big[off:off + n]
-        dQ = torch.from_numpy(Q).to(cuda)
-        with R.RMQIndex(dA, 1000) as ix:
-            assert ix.info()["aligned"] == 0
-            v, i = ix.query(dQ)
-            torch.cuda.synchronize()
-        Ah = A[off:off + n]
-        np.testing.assert_array_equal(i.cpu().numpy(), oracle_lib.base_idx(Ah, Q))
-        np.testing.assert_array_equal(bits(v.cpu().numpy()), bits(oracle_lib.base_val(Ah, Q)))
+        for bs in (1000, 1024):
+            dA = big[off:off + n]
+            dQ = torch.from_numpy(Q).to(cuda)
+            with R.RMQIndex(dA, bs) as ix:
+                assert ix.info()["aligned"] == 0
+                v, i = ix.query(dQ)
+                torch.cuda.synchronize()
+            Ah = A[off:off + n]
+            np.testing.assert_array_equal(i.cpu().numpy(), oracle_lib.base_idx(Ah, Q))
+            np.testing.assert_array_equal(bits(v.cpu().numpy()), bits(oracle_lib.base_val(Ah, Q)))
 
 
 def test_invalid_queries(cuda, native):
