@@ -124,6 +124,26 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
 int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q,
                    float *h_val, int32_t *h_idx, rmq_stream_t stream);
 
+/*
+ * Build + query of one array in one call that allocates nothing. No
+ * counterpart in the reference: it exists for callers that may not allocate
+ * device memory (a host framework that owns all device memory through its
+ * own pool, or a latency-critical loop that cannot take the implicit
+ * device-wide synchronisation of cudaMalloc / cudaFree). The index is built
+ * into a fixed device array inside this library (RMQ_NOALLOC_SCRATCH_BYTES,
+ * held on every GPU that loads the library until the process exits) and the
+ * queries are answered from it; the caller passes inputs and outputs as for
+ * rmq_build + rmq_query, with the same results. Sizes whose index does not
+ * fit are rejected with RMQ_EINVAL (any n <= 2^20 fits for bs >= 16).
+ * The first call on a device looks up the array's device address (set-up),
+ * so make that first call before any stream capture. All calls share the
+ * array: calls whose work overlaps on the GPU race.
+ */
+#define RMQ_NOALLOC_SCRATCH_BYTES (32u << 20)
+int rmq_query_noalloc(const float *d_vals, int64_t n, int64_t bs,
+                      const int32_t *d_queries, int64_t q, float *d_val,
+                      int32_t *d_idx, rmq_stream_t stream);
+
 /* Release everything the handle owns. NULL is accepted. */
 int rmq_free(rmq_handle_t *h);
 

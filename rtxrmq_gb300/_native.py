@@ -57,6 +57,7 @@ SIGNATURES = {
     "rmq_build_ex": (C.c_int, [_vp, _i64, _i64, C.c_uint32, _vp, C.POINTER(_vp)]),
     "rmq_query": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "rmq_query_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "rmq_query_noalloc": (C.c_int, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_free": (C.c_int, [_vp]),
     "rmq_info": (C.c_int, [_vp, C.POINTER(rmq_info_t)]),
     "rmq_invalid_count": (C.c_int, [_vp, _vp, C.POINTER(_i64)]),

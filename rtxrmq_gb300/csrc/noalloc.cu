@@ -1,0 +1,131 @@
+// noalloc.cu -- build + query of one array in a single call that allocates
+// nothing: the index lives in a fixed device array owned by this library.
+//
+// Who needs it: callers that are not allowed to allocate device memory
+// themselves or through a library -- a host framework that accounts for all
+// device memory through its own pool and forbids third-party cudaMalloc, or
+// a latency-critical loop that cannot take cudaMalloc / cudaFree's implicit
+// device-wide synchronisation. They pass their own input and output buffers;
+// the prefix/suffix minima, sparse tables and invalid-query counter are
+// written into g_noalloc_scratch below instead of memory from rmq_build.
+//
+// The array is a file-scope __device__ variable of kNoallocScratchBytes, so
+// every GPU that loads this library holds it until the process exits. In
+// host code its name is only a host-side stand-in, never a device address:
+// the device address comes from cudaGetSymbolAddress, called once per device
+// with that device current (first call of rmq_query_noalloc on the device).
+// All calls share the array and it keeps the last call's contents; the
+// counter is cleared by every call and everything else is rewritten before
+// it is read. Calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on the array.
+#include <cstring>
+#include <mutex>
+
+#include "../../include/rmq.h"
+#include "engine.h"
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[RMQ_NOALLOC_SCRATCH_BYTES];
+
+namespace rmq {
+namespace {
+
+constexpr size_t kNoallocScratchBytes = static_cast<size_t>(RMQ_NOALLOC_SCRATCH_BYTES);
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set-up on the
+// first call per device).
+int scratch_address(int device, void **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (err != cudaSuccess || !p) {
+            cudaGetLastError();
+            return set_error(RMQ_ECUDA, "rmq_query_noalloc: cudaGetSymbolAddress failed: %s",
+                             cudaGetErrorString(err));
+        }
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return RMQ_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+}  // namespace
+}  // namespace rmq
+
+using namespace rmq;
+
+extern "C" int rmq_query_noalloc(const float *d_vals, int64_t n, int64_t bs,
+                                 const int32_t *d_queries, int64_t q, float *d_val,
+                                 int32_t *d_idx, rmq_stream_t stream) {
+    if (n <= 0 || n > 0x7fffffffLL)
+        return set_error(RMQ_EINVAL, "rmq_query_noalloc: n=%lld outside [1, 2^31-1]", (long long)n);
+    if (!d_vals || reinterpret_cast<uintptr_t>(d_vals) % 4)
+        return set_error(RMQ_EINVAL, "rmq_query_noalloc: d_vals NULL or not 4-byte aligned");
+    if (q < 0) return set_error(RMQ_EINVAL, "rmq_query_noalloc: q=%lld < 0", (long long)q);
+    if (q > 0 && (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8))
+        return set_error(RMQ_EINVAL, "rmq_query_noalloc: d_queries NULL or not 8-byte aligned");
+    if (q > 0 && !d_val && !d_idx)
+        return set_error(RMQ_EINVAL, "rmq_query_noalloc: both outputs are NULL");
+    if ((d_val && reinterpret_cast<uintptr_t>(d_val) % 4) ||
+        (d_idx && reinterpret_cast<uintptr_t>(d_idx) % 4))
+        return set_error(RMQ_EINVAL, "rmq_query_noalloc: outputs not 4-byte aligned");
+    if (bs <= 0) bs = RMQ_DEFAULT_BS;
+    if (bs > n) bs = n;
+
+    BuildPlan p;
+    p.A = d_vals;
+    p.n = static_cast<uint32_t>(n);
+    p.bs = static_cast<uint32_t>(bs);
+    p.nb = static_cast<uint32_t>((n + bs - 1) / bs);
+    p.levels = st_levels(p.nb);
+    p.aligned = reinterpret_cast<uintptr_t>(d_vals) % 16 == 0;
+    p.mlevels = micro_levels(p.bs);
+    p.micro = p.mlevels > 0;
+    p.nmicro = p.micro ? static_cast<uint32_t>((n + kMicro - 1) / kMicro) : 0u;
+
+    const size_t pre_b = align256(sizeof(Entry) * static_cast<size_t>(n));
+    const size_t st_b = align256(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels);
+    const size_t mst_b = align256(sizeof(Entry) * static_cast<size_t>(p.nmicro) * p.mlevels);
+    const size_t need = 2 * pre_b + st_b + mst_b + 256;
+    if (need > kNoallocScratchBytes)
+        return set_error(RMQ_EINVAL,
+                         "rmq_query_noalloc: n=%lld with bs=%lld needs %zu bytes of scratch; the "
+                         "static scratch holds %zu bytes (use rmq_build / rmq_query)",
+                         (long long)n, (long long)bs, need, kNoallocScratchBytes);
+
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    if (dev.device >= kMaxDevices)
+        return set_error(RMQ_ENOTSUP, "rmq_query_noalloc: device %d unsupported", dev.device);
+    void *base_v = nullptr;
+    rc = scratch_address(dev.device, &base_v);
+    if (rc) return rc;
+    char *base = static_cast<char *>(base_v);
+    p.pre = reinterpret_cast<Entry *>(base);
+    p.suf = reinterpret_cast<Entry *>(base + pre_b);
+    p.st = reinterpret_cast<Entry *>(base + 2 * pre_b);
+    p.mst = p.micro ? reinterpret_cast<Entry *>(base + 2 * pre_b + st_b) : nullptr;
+    unsigned long long *invalid =
+        reinterpret_cast<unsigned long long *>(base + 2 * pre_b + st_b + mst_b);
+
+    cudaError_t err = cudaMemsetAsync(invalid, 0, sizeof(unsigned long long), stream);
+    if (err == cudaSuccess) err = launch_build(p, dev, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_query_noalloc: build");
+    if (q == 0) return RMQ_OK;
+    QueryArgs a;
+    a.Q = reinterpret_cast<const int2 *>(d_queries);
+    a.q = q;
+    a.val = d_val;
+    a.idx = d_idx;
+    a.invalid = invalid;
+    err = launch_query(p, a, dev, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_query_noalloc: query");
+    return RMQ_OK;
+}
