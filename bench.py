@@ -60,7 +60,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--bs", type=int, default=0, help="fixed block size (skips the sweep)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end step")
+    ap.add_argument("--skip-plain", action="store_true", help="skip the plain modes (headline)")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--batch-bs", type=int, default=0,
+                    help="fixed block size for every bucket (skips the autotuner)")
     ap.add_argument("--skip-autograd", action="store_true")
     ap.add_argument("--batch-arrays", type=int, default=4096)
     ap.add_argument("--batch-q", type=int, default=1 << 26)
@@ -285,8 +288,11 @@ def bench_batched(args, dev, stream, barrier):
     ov = torch.empty(w.total_q, dtype=torch.float32, device=dev)
     oi = torch.empty(w.total_q, dtype=torch.int32, device=dev)
     t = time.perf_counter()
-    cfg = autotune(w.starts, w.lengths, w.qstarts, w.qcounts, dV, dQ, reps=2,
-                   queries_host=w.queries, cache=None)
+    if args.batch_bs:
+        cfg = [args.batch_bs] * 32
+    else:
+        cfg = autotune(w.starts, w.lengths, w.qstarts, w.qcounts, dV, dQ, reps=2,
+                       queries_host=w.queries, cache=None)
     tune_s = time.perf_counter() - t
     res = {"workload": "4096 arrays, len round(2^U) U~U[8,22], 2^26 queries proportional to "
                        "length, query len lognormal(0.5 ln len, 0.4), values U[0,1)",
@@ -410,6 +416,8 @@ def main():
     A = R.gen_values_uniform(n, SEED)
     dA = torch.from_numpy(A).to(dev)
     modes = MODES if args.modes == "all" else [(f"lr={m}", int(m)) for m in args.modes.split(",")]
+    if args.skip_plain:
+        modes = []
     out_v = torch.empty(q, dtype=torch.float32, device=dev)
     out_i = torch.empty(q, dtype=torch.int32, device=dev)
 
@@ -489,6 +497,12 @@ def main():
     clocks = sampler.summary()
 
     if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    if not results:  # a run of the batched / autograd sections only
+        print(json.dumps({"metric": "batched / differentiable sections only", "value": None,
+                          "clocks": clocks, "batched": batched, "autograd": autograd}), flush=True)
         if world > 1:
             dist.destroy_process_group()
         return

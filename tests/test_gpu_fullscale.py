@@ -1,0 +1,84 @@
+"""GPU parity at the benchmark sizes.
+
+Plain RMQ at n = 1e8, q = 2^26 for every length mode, and the tie-heavy
+configuration (n = 2^27 integers in [0,256), q = 2^26, fixed lengths
+1 .. 2^22). Brute force over 2^26 queries is out of reach on the CPU, so:
+  * every answer is checked for size-independent properties: l <= idx <= r
+    and the value is bit-identical to A[idx];
+  * a random sample of answers is checked exactly (index and value bits)
+    against the CPU oracle's restatement of the reference's block
+    decomposition, and for short lengths against BASE itself.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def check_properties(A, Q, v, i):
+    l, r = Q[:, 0], Q[:, 1]
+    assert (i >= l).all() and (i <= r).all(), "index outside its range"
+    np.testing.assert_array_equal(A[i].view(np.uint32), v.view(np.uint32))
+
+
+def sampled_exact(oracle_lib, A, Q, v, i, m, seed, base=False):
+    rng = np.random.default_rng(seed)
+    s = rng.integers(0, len(Q), m)
+    if base:
+        ev, ei = oracle_lib.base_val(A, Q[s]), oracle_lib.base_idx(A, Q[s])
+    else:
+        ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q[s])
+    np.testing.assert_array_equal(i[s], ei)
+    np.testing.assert_array_equal(v[s].view(np.uint32), ev.view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def plain_data(cuda, native):
+    import torch
+
+    import rtxrmq_gb300 as R
+    A = R.gen_values_uniform(10**8, 1321)
+    return A, torch.from_numpy(A).to(cuda)
+
+
+@pytest.mark.parametrize("lr", [-1, -2, -3, 1024])
+def test_plain_n1e8_q2e26(cuda, native, oracle_lib, plain_data, lr):
+    import torch
+
+    import rtxrmq_gb300 as R
+    A, dA = plain_data
+    Q = R.gen_queries(1 << 26, len(A), lr, 1322)
+    dQ = torch.from_numpy(Q).to(cuda)
+    with R.RMQIndex(dA, 4096) as ix:
+        v, i = ix.query(dQ)
+        torch.cuda.synchronize()
+        assert ix.invalid_count() == 0
+    v, i = v.cpu().numpy(), i.cpu().numpy()
+    check_properties(A, Q, v, i)
+    sampled_exact(oracle_lib, A, Q, v, i, 1 << 14, 7)
+    if lr in (-3, 1024):
+        sampled_exact(oracle_lib, A, Q, v, i, 1 << 18, 8, base=True)
+
+
+@pytest.mark.parametrize("length", [1, 32, 1 << 10, 1 << 16, 1 << 22])
+def test_tie_heavy_n2e27_q2e26(cuda, native, oracle_lib, length):
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = 1 << 27
+    A = R.gen_values_int(n, 256, 1321)
+    Q = R.gen_queries(1 << 26, n, length, 1323)
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    with R.RMQIndex(dA, 4096) as ix:
+        v, i = ix.query(dQ)
+        torch.cuda.synchronize()
+    v, i = v.cpu().numpy(), i.cpu().numpy()
+    check_properties(A, Q, v, i)
+    # leftmost: nothing in [l, idx) equals the minimum (sampled; the sampled
+    # exact comparison below covers it too)
+    sampled_exact(oracle_lib, A, Q, v, i, 1 << 13, 9)
+    if length <= 1 << 10:
+        sampled_exact(oracle_lib, A, Q, v, i, 1 << 16, 10, base=True)
+    del dA, dQ
+    torch.cuda.empty_cache()
