@@ -18,9 +18,9 @@ roofline   -- algorithmic HBM bytes per launch (query read + result write +
               one 32-byte sector per pre/suf lookup, 32 bytes per sector a
               block scan touches) / kernel time, against the measured copy
               bandwidth.
-cpu_baseline -- the CPU oracle's restatement of the reference's
-              block-decomposition path on this host's cores, on a bounded
-              sample of the same queries.
+cpu_baseline -- the reference's CPU comparator HRMQ (restated in the
+              oracle, hrmq_port.c) on this host's cores, on a bounded sample
+              of the same queries.
 
 `--impl reference` times that CPU path alone (rank 0) and prints its own line.
 """
@@ -188,34 +188,37 @@ def time_steps(fn, steps, warmup, stream, barrier):
 
 # ---------------------------------------------------------------- CPU side
 
-def cpu_sample_rate(A, Q, bs, target_s=12.0, nt=0):
-    """Oracle port of RTX_blocks on the host cores over a bounded query sample."""
+CPU_KIND = ("HRMQ restated (oracle/hrmq_port.c: balanced-parentheses RMQ of the reference's "
+            "hrmq/RMQRMM64.cpp, ties leftmost), queries on all host threads")
+
+
+def cpu_sample_rate(A, Q, target_s=12.0, nt=0):
+    """The reference's CPU comparator (HRMQ, restated) on the host cores over
+    a bounded random sample of the step's queries; build timed apart."""
     import oracle
     nt = nt or os.cpu_count() or 1
     t = time.perf_counter()
-    ob = oracle.Blocks(A, bs, nt)
+    h = oracle.HRMQ(A, strict=True, nt=nt)
     build_s = time.perf_counter() - t
     rng = np.random.default_rng(5)
-    probe = Q[rng.integers(0, len(Q), 2048)]
+    probe = Q[rng.integers(0, len(Q), 4096)]
     t = time.perf_counter()
-    ob.query(probe, nt)
+    h.query(probe, nt)
     per = (time.perf_counter() - t) / len(probe)
     m = int(min(len(Q), max(4096, target_s / max(per, 1e-9))))
     sample = Q[rng.integers(0, len(Q), m)]
     t = time.perf_counter()
-    ob.query(sample, nt)
+    h.query(sample, nt)
     dt = time.perf_counter() - t
-    ob.close()
+    h.close()
     return m / dt, {"cores": nt, "sample": f"{m} random queries of the step's query set "
-                    f"(n={len(A)}, bs={bs}), {dt:.1f} s", "construction_s": build_s}
-
-
-def cpu_bs(n):
-    # block size minimising bs + n/bs per query for the O(bs + nb) CPU path
-    return int(max(1, round(n ** 0.5)))
+                    f"(n={len(A)}), {dt:.1f} s; construction {build_s:.2f} s", "construction_s": build_s}
 
 
 def run_reference(args, rank):
+    """--impl reference: the reference's CPU path for this workload (HRMQ,
+    restated in the oracle; the reference's compiled code cannot run on the
+    GPU host), rank 0 only, every step a bounded sample of the queries."""
     if rank != 0:
         return
     import oracle
@@ -225,21 +228,22 @@ def run_reference(args, rank):
     n, q = args.n, args.q
     A = R.gen_values_uniform(n, SEED)
     Q = R.gen_queries(q, n, -1, SEED + 1)
-    bs = cpu_bs(n)
-    ob = oracle.Blocks(A, bs, nt)
-    rng = np.random.default_rng(9)
-    probe = Q[rng.integers(0, q, 1024)]
     t = time.perf_counter()
-    ob.query(probe, nt)
+    h = oracle.HRMQ(A, strict=True, nt=nt)
+    build_s = time.perf_counter() - t
+    rng = np.random.default_rng(9)
+    probe = Q[rng.integers(0, q, 4096)]
+    t = time.perf_counter()
+    h.query(probe, nt)
     per = (time.perf_counter() - t) / len(probe)
-    m = int(max(1024, min(q, 1.5 / max(per, 1e-9))))  # ~1.5 s of work per step
+    m = int(max(4096, min(q, 1.5 / max(per, 1e-9))))  # ~1.5 s of work per step
     for _ in range(args.warmup):
-        ob.query(Q[rng.integers(0, q, m)], nt)
+        h.query(Q[rng.integers(0, q, m)], nt)
     times = []
     for _ in range(args.steps):
         s = Q[rng.integers(0, q, m)]
         t = time.perf_counter()
-        ob.query(s, nt)
+        h.query(s, nt)
         times.append(time.perf_counter() - t)
     v = m * args.steps / sum(times)
     line = {"metric": "RMQ/s n=1e8 q=2^26 lr=-1 (values+indices)", "value": v, "unit": "RMQ/s",
@@ -249,8 +253,8 @@ def run_reference(args, rank):
             "config": {"workload": "plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices",
                        "n": n, "q": q, "lr": -1, "seed": SEED},
             "cpu_baseline": {"value": v, "unit": "RMQ/s", "cores": nt, "kind": "port",
-                             "sample": f"{m} random queries per step from the 2^26-query set, "
-                                       f"oracle restatement of RTX_blocks (bs={bs}) on {nt} threads"},
+                             "sample": f"{m} random queries per step from the 2^26-query set; "
+                                       f"{CPU_KIND}; construction {build_s:.2f} s"},
             "e2e": {"value": v, "unit": "RMQ/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -533,10 +537,9 @@ def main():
         "autograd": autograd,
     }
     if not args.no_cpu and world == 1:
-        cbs = cpu_bs(n)
-        v, meta = cpu_sample_rate(A, Q, cbs)
+        v, meta = cpu_sample_rate(A, Q)
         line["cpu_baseline"] = {"value": v, "unit": "RMQ/s", "cores": meta["cores"], "kind": "port",
-                                "sample": meta["sample"]}
+                                "sample": meta["sample"] + "; " + CPU_KIND}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -58,6 +58,12 @@ def lib() -> C.CDLL:
         L.oracle_blocks_query.argtypes = [_vp, _vp, _i64, _vp, _vp, _i32]
         L.oracle_blocks_free.argtypes = [_vp]
         L.oracle_max_threads.restype = _i32
+        L.hrmq_port_build.restype = _vp
+        L.hrmq_port_build.argtypes = [_vp, _i64, _i32, _i32]
+        L.hrmq_port_query.argtypes = [_vp, _vp, _vp, _i64, _vp, _vp, _i32]
+        L.hrmq_port_bytes.restype = _i64
+        L.hrmq_port_bytes.argtypes = [_vp]
+        L.hrmq_port_free.argtypes = [_vp]
         _lib = L
     return _lib
 
@@ -112,6 +118,41 @@ class Blocks:
     def close(self):
         if self._h:
             lib().oracle_blocks_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class HRMQ:
+    """The reference's CPU comparator HRMQ (hrmq/RMQRMM64.cpp) restated in
+    hrmq_port.c: balanced-parentheses RMQ. strict=False resolves ties
+    rightmost (as HRMQ), strict=True leftmost (as BASE)."""
+
+    def __init__(self, A, strict: bool = False, nt: int = 0):
+        self.A, pa = _arr(A, np.float32)
+        self._h = lib().hrmq_port_build(pa, len(self.A), int(bool(strict)), nt)
+        if not self._h:
+            raise MemoryError("hrmq_port_build failed")
+
+    def query(self, Q, nt: int = 0):
+        Q, pq = _arr(Q, np.int32)
+        val = np.empty(len(Q), dtype=np.float32)
+        idx = np.empty(len(Q), dtype=np.int32)
+        if lib().hrmq_port_query(self._h, self.A.ctypes.data, pq, len(Q), val.ctypes.data,
+                                 idx.ctypes.data, nt) != 0:
+            raise ValueError("hrmq_port_query: bad arguments")
+        return val, idx
+
+    def nbytes(self) -> int:
+        return lib().hrmq_port_bytes(self._h)
+
+    def close(self):
+        if self._h:
+            lib().hrmq_port_free(self._h)
             self._h = None
 
     def __del__(self):

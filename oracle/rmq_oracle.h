@@ -23,6 +23,15 @@ void oracle_blocks_free(oracle_blocks_t *o);
 
 int oracle_max_threads(void);
 
+/* HRMQ (hrmq/RMQRMM64.cpp) restated: balanced-parentheses RMQ. strict = 0
+ * resolves ties rightmost like HRMQ, strict = 1 leftmost like BASE. */
+typedef struct hrmq_port hrmq_port_t;
+hrmq_port_t *hrmq_port_build(const float *A, int64_t n, int strict, int nt);
+int hrmq_port_query(const hrmq_port_t *h, const float *A, const int32_t *Q, int64_t q, float *val,
+                    int32_t *idx, int nt);
+int64_t hrmq_port_bytes(const hrmq_port_t *h);
+void hrmq_port_free(hrmq_port_t *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,3 +71,34 @@ def test_live_against_reference(oracle_lib, native):
         np.testing.assert_array_equal(oracle_lib.base_idx(A, Q), oracle_lib.ref_cpu_rmq_idx(A, Q))
         v, i = oracle_lib.Blocks(A, 64 + seed).query(Q)
         np.testing.assert_array_equal(i, oracle_lib.ref_cpu_rmq_idx(A, Q))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: p.stem)
+def test_hrmq_port_matches_reference_hrmq(path, oracle_lib):
+    """oracle/hrmq_port.c (HRMQ restated) reproduces the reference HRMQ's
+    native indices (rightmost on ties) wherever the fixture has them, and
+    BASE's leftmost indices and value bits in strict mode."""
+    g = np.load(path)
+    A, Q = g["A"], g["Q"]
+    if "hrmq_idx" in g:
+        v, i = oracle_lib.HRMQ(A, strict=False).query(Q)
+        np.testing.assert_array_equal(i, g["hrmq_idx"])
+        np.testing.assert_array_equal(bits(v), bits(g["hrmq_val"]))
+    v, i = oracle_lib.HRMQ(A, strict=True).query(Q)
+    np.testing.assert_array_equal(i, g["base_idx"])
+    np.testing.assert_array_equal(bits(v), bits(g["base_val"]))
+
+
+def test_hrmq_port_large_random(oracle_lib, native):
+    """n = 2^20 with heavy ties, every length class: strict mode equals the
+    block restatement; native mode returns a minimum at or right of it."""
+    import rtxrmq_gb300 as R
+    n = 1 << 20
+    A = R.gen_values_int(n, 64, 17)
+    Q = np.concatenate([R.gen_queries(4000, n, L, 3) for L in (-1, -2, -3, 1, 2, 64, 1000)])
+    ev, ei = oracle_lib.Blocks(A, 4096).query(Q)
+    v, i = oracle_lib.HRMQ(A, strict=True).query(Q)
+    np.testing.assert_array_equal(i, ei)
+    v2, i2 = oracle_lib.HRMQ(A, strict=False).query(Q)
+    np.testing.assert_array_equal(bits(v2), bits(ev))
+    assert (i2 >= ei).all() and (i2 <= Q[:, 1]).all()
