@@ -155,13 +155,14 @@ def algorithmic_bytes(Q: np.ndarray, n: int, bs: int, out_bytes: int) -> tuple[f
     total = per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge.sum()
     micro = bs % 32 == 0 and bs >= 64
     if micro:
-        # sub-block level: the partial 32-element micro-blocks at both ends,
-        # plus two micro-table entries when micro-blocks lie between
+        # sub-block level: inside one 32-element micro-block a scan of its
+        # line; otherwise one sector each for the in-micro-block suffix at l
+        # and prefix at r, plus two micro-table entries when micro-blocks lie
+        # between
         ls, rs = l[scan], r[scan]
         ml, mr = ls // 32, rs // 32
         one = ml == mr
-        sec = np.where(one, sectors(ls, rs),
-                       sectors(ls, ml * 32 + 31) + sectors(mr * 32, rs) + 2 * (mr - ml >= 2))
+        sec = np.where(one, sectors(ls, rs), 2 + 2 * (mr - ml >= 2))
     else:
         sec = sectors(l[scan], r[scan])
     total += 32.0 * sec.sum()

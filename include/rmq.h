@@ -83,10 +83,12 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
 
 /*
  * rmq_build with options. When bs is a multiple of 32 (and >= 64) the index
- * also gets a sub-block level -- minima of 32-element micro-blocks and a
- * sparse table over them, truncated to windows shorter than one block -- so
- * that a query inside one block reads two 128-byte lines and two table
- * entries instead of scanning A[l..r]. RMQ_BUILD_NO_MICRO leaves it out.
+ * also gets a sub-block level -- prefix and suffix minima inside 32-element
+ * micro-blocks (16 more bytes per element) and a sparse table over the
+ * micro-block minima, truncated to windows shorter than one block -- so
+ * that a query inside one block reads two entries and at most two table
+ * entries (one 128-byte line if it lies inside one micro-block) instead of
+ * scanning A[l..r]. RMQ_BUILD_NO_MICRO leaves it out.
  * rmq_build(...) is rmq_build_ex(..., 0, ...).
  */
 int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags,

@@ -112,20 +112,11 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     if (rc) return rc;
 
     BuildPlan p;
+    std::memset(&p, 0, sizeof(p));
     p.A = d_vals;
     p.n = static_cast<uint32_t>(n);
     p.bs = static_cast<uint32_t>(bs);
-    p.nb = static_cast<uint32_t>((n + bs - 1) / bs);
-    p.levels = st_levels(p.nb);
-    p.aligned = (reinterpret_cast<uintptr_t>(d_vals) % 16) == 0;
-    p.mlevels = (flags & RMQ_BUILD_NO_MICRO) ? 0u : micro_levels(p.bs);
-    p.micro = p.mlevels > 0;
-    p.nmicro = p.micro ? static_cast<uint32_t>((n + kMicro - 1) / kMicro) : 0u;
-
-    const size_t pre_b = align_up(sizeof(Entry) * static_cast<size_t>(n), 256);
-    const size_t st_b = align_up(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels, 256);
-    const size_t mst_b = align_up(sizeof(Entry) * static_cast<size_t>(p.nmicro) * p.mlevels, 256);
-    const size_t total = 2 * pre_b + st_b + mst_b + 256;
+    const size_t total = plan_index(p, (flags & RMQ_BUILD_NO_MICRO) != 0);
 
     rmq_handle_t *h = new (std::nothrow) rmq_handle_t;
     if (!h) return set_error(RMQ_ENOMEM, "rmq_build: host allocation failed");
@@ -138,12 +129,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
         return set_error(RMQ_ENOMEM, "rmq_build: cudaMalloc(%zu bytes) failed: %s", total,
                          cudaGetErrorString(err));
     }
-    char *base = static_cast<char *>(h->mem);
-    p.pre = reinterpret_cast<Entry *>(base);
-    p.suf = reinterpret_cast<Entry *>(base + pre_b);
-    p.st = reinterpret_cast<Entry *>(base + 2 * pre_b);
-    p.mst = p.micro ? reinterpret_cast<Entry *>(base + 2 * pre_b + st_b) : nullptr;
-    h->invalid = reinterpret_cast<unsigned long long *>(base + 2 * pre_b + st_b + mst_b);
+    h->invalid = place_index(p, h->mem);
     h->mem_bytes = total;
     h->table_bytes = static_cast<int64_t>(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels);
     h->plan = p;

@@ -81,6 +81,8 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     v.st = P.ws + a.st;
     v.mst = nullptr;  // batched arrays answer same-block queries with warp scans
     v.nmicro = 0;
+    v.mpre = nullptr;
+    v.msuf = nullptr;
     return v;
 }
 
@@ -395,6 +397,8 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
         p.nmicro = 0;
         p.mlevels = 0;
         p.mst = nullptr;
+        p.mpre = nullptr;
+        p.msuf = nullptr;
         cudaError_t err = launch_build(p, dev, stream);
         if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run_per_array: build");
         if (qcount[i] == 0) continue;

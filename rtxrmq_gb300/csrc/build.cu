@@ -32,47 +32,36 @@ __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
         cur[j] = better(prev[j], prev[j + half]);
 }
 
-// Leftmost minimum of every 32-element micro-block, one thread per block
-// reading its 128-byte line with float4 loads.
-template <bool ALIGNED>
+// Sub-block level, one warp per 32-element micro-block (lane = element):
+// in-micro-block prefix and suffix minima by warp shuffles, written with
+// coalesced 256-byte stores, and the micro-block minimum (suffix minimum at
+// its first element) as level 0 of the micro table.
 __global__ void __launch_bounds__(256)
-micro_min_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entry *mst0) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nmicro;
-         j += gridDim.x * blockDim.x) {
-        const uint32_t a = j * kMicro;
-        const uint32_t b = min(a + kMicro, n);
-        uint64_t best = ~0ull;
-        uint32_t best_bits = 0u;
-        if (ALIGNED && b == a + kMicro) {
-            const float4 *src = reinterpret_cast<const float4 *>(A + a);
+micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entry *mpre,
+                  Entry *msuf, Entry *mst0) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < nmicro; j += warps) {
+        const uint32_t g = j * kMicro + lane;
+        const bool in = g < n;
+        const uint32_t bits = in ? __float_as_uint(__ldg(A + g)) : 0u;
+        const uint64_t c = in ? ((static_cast<uint64_t>(fkey(bits)) << 32) | g) : ~0ull;
+        uint64_t p = c, s = c;
 #pragma unroll
-            for (int v = 0; v < 8; ++v) {
-                const float4 f = __ldg(src + v);
-                const uint32_t w[4] = {__float_as_uint(f.x), __float_as_uint(f.y),
-                                       __float_as_uint(f.z), __float_as_uint(f.w)};
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const uint64_t k = (static_cast<uint64_t>(fkey(w[c])) << 32) | (a + 4 * v + c);
-                    if (k < best) {
-                        best = k;
-                        best_bits = w[c];
-                    }
-                }
-            }
-        } else {
-            for (uint32_t g = a; g < b; ++g) {
-                const uint32_t w = __float_as_uint(__ldg(A + g));
-                const uint64_t k = (static_cast<uint64_t>(fkey(w)) << 32) | g;
-                if (k < best) {
-                    best = k;
-                    best_bits = w;
-                }
-            }
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t tp = __shfl_up_sync(0xffffffffu, p, o);
+            const uint64_t ts = __shfl_down_sync(0xffffffffu, s, o);
+            if (lane >= static_cast<uint32_t>(o) && tp < p) p = tp;
+            if (lane + o < 32u && ts < s) s = ts;
         }
-        Entry e;
-        e.bits = best_bits;
-        e.idx = static_cast<uint32_t>(best);
-        mst0[j] = e;
+        // raw bits of each argmin come from the lane that holds it
+        const uint32_t pb = __shfl_sync(0xffffffffu, bits, static_cast<uint32_t>(p) & 31u);
+        const uint32_t sb = __shfl_sync(0xffffffffu, bits, static_cast<uint32_t>(s) & 31u);
+        if (in) {
+            __stcs(reinterpret_cast<uint2 *>(mpre + g), make_uint2(pb, static_cast<uint32_t>(p)));
+            __stcs(reinterpret_cast<uint2 *>(msuf + g), make_uint2(sb, static_cast<uint32_t>(s)));
+            if (lane == 0) mst0[j] = Entry{sb, static_cast<uint32_t>(s)};
+        }
     }
 }
 
@@ -95,6 +84,48 @@ cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceI
 }  // namespace
 
 uint32_t st_levels(uint32_t nb) { return nb ? static_cast<uint32_t>(ilog2(nb)) + 1u : 0u; }
+
+namespace {
+size_t a256(size_t x) { return (x + 255) / 256 * 256; }
+struct Offsets {
+    size_t pre, suf, st, mst, mpre, msuf, counter, total;
+};
+Offsets offsets_of(const BuildPlan &p) {
+    Offsets o;
+    const size_t nent = a256(sizeof(Entry) * static_cast<size_t>(p.n));
+    o.pre = 0;
+    o.suf = nent;
+    o.st = 2 * nent;
+    o.mst = o.st + a256(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels);
+    o.mpre = o.mst + a256(sizeof(Entry) * static_cast<size_t>(p.nmicro) * p.mlevels);
+    o.msuf = o.mpre + (p.micro ? nent : 0);
+    o.counter = o.msuf + (p.micro ? nent : 0);
+    o.total = o.counter + 256;
+    return o;
+}
+}  // namespace
+
+size_t plan_index(BuildPlan &p, bool no_micro) {
+    p.nb = (p.n + p.bs - 1) / p.bs;
+    p.levels = st_levels(p.nb);
+    p.mlevels = no_micro ? 0u : micro_levels(p.bs);
+    p.micro = p.mlevels > 0;
+    p.nmicro = p.micro ? (p.n + kMicro - 1) / kMicro : 0u;
+    p.aligned = reinterpret_cast<uintptr_t>(p.A) % 16 == 0;
+    return offsets_of(p).total;
+}
+
+unsigned long long *place_index(BuildPlan &p, void *base_v) {
+    char *base = static_cast<char *>(base_v);
+    const Offsets o = offsets_of(p);
+    p.pre = reinterpret_cast<Entry *>(base + o.pre);
+    p.suf = reinterpret_cast<Entry *>(base + o.suf);
+    p.st = reinterpret_cast<Entry *>(base + o.st);
+    p.mst = p.micro ? reinterpret_cast<Entry *>(base + o.mst) : nullptr;
+    p.mpre = p.micro ? reinterpret_cast<Entry *>(base + o.mpre) : nullptr;
+    p.msuf = p.micro ? reinterpret_cast<Entry *>(base + o.msuf) : nullptr;
+    return reinterpret_cast<unsigned long long *>(base + o.counter);
+}
 
 uint32_t micro_levels(uint32_t bs) {
     if (bs < 2 * kMicro || bs % kMicro) return 0;
@@ -138,13 +169,10 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     err = launch_levels(p.st, p.nb, p.levels, dev, s);
     if (err != cudaSuccess || !p.micro) return err;
 
-    uint32_t g = (p.nmicro + 255) / 256;
-    const uint32_t cap = static_cast<uint32_t>(dev.sms) * 16u;
+    uint32_t g = (p.nmicro + 7) / 8;  // 8 warps per CTA, one micro-block per warp
+    const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
     if (g > cap) g = cap;
-    if (p.aligned)
-        micro_min_kernel<true><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mst);
-    else
-        micro_min_kernel<false><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mst);
+    micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     return launch_levels(p.mst, p.nmicro, p.mlevels, dev, s);

@@ -41,10 +41,19 @@ struct BuildPlan {
     uint32_t nmicro;   // ceil(n / 32)
     uint32_t mlevels;
     Entry *mst;        // [mlevels * nmicro]
+    Entry *mpre;       // [n] leftmost minimum of A[microstart(i) .. i]
+    Entry *msuf;       // [n] leftmost minimum of A[i .. microend(i)]
 };
 constexpr uint32_t kMicro = 32;
 // levels of the micro table for block size bs (0 when not applicable)
 uint32_t micro_levels(uint32_t bs);
+
+// Fill the size fields of a plan (A, n, bs given; micro level on unless
+// `no_micro`); returns the bytes of the single allocation holding the index
+// and its invalid-query counter.
+size_t plan_index(BuildPlan &p, bool no_micro);
+// Point the plan's arrays into that allocation; returns the counter.
+unsigned long long *place_index(BuildPlan &p, void *base);
 uint32_t st_levels(uint32_t nb);
 cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s);
 

@@ -53,8 +53,6 @@ int scratch_address(int device, void **out) {
     return RMQ_OK;
 }
 
-size_t align256(size_t x) { return (x + 255) / 256 * 256; }
-
 }  // namespace
 }  // namespace rmq
 
@@ -79,20 +77,13 @@ extern "C" int rmq_query_noalloc(const float *d_vals, int64_t n, int64_t bs,
     if (bs > n) bs = n;
 
     BuildPlan p;
+    std::memset(&p, 0, sizeof(p));
     p.A = d_vals;
     p.n = static_cast<uint32_t>(n);
     p.bs = static_cast<uint32_t>(bs);
-    p.nb = static_cast<uint32_t>((n + bs - 1) / bs);
-    p.levels = st_levels(p.nb);
-    p.aligned = reinterpret_cast<uintptr_t>(d_vals) % 16 == 0;
-    p.mlevels = micro_levels(p.bs);
-    p.micro = p.mlevels > 0;
-    p.nmicro = p.micro ? static_cast<uint32_t>((n + kMicro - 1) / kMicro) : 0u;
-
-    const size_t pre_b = align256(sizeof(Entry) * static_cast<size_t>(n));
-    const size_t st_b = align256(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels);
-    const size_t mst_b = align256(sizeof(Entry) * static_cast<size_t>(p.nmicro) * p.mlevels);
-    const size_t need = 2 * pre_b + st_b + mst_b + 256;
+    // the sub-block level when it fits, otherwise the plain index (same results)
+    size_t need = plan_index(p, false);
+    if (need > kNoallocScratchBytes) need = plan_index(p, true);
     if (need > kNoallocScratchBytes)
         return set_error(RMQ_EINVAL,
                          "rmq_query_noalloc: n=%lld with bs=%lld needs %zu bytes of scratch; the "
@@ -104,16 +95,10 @@ extern "C" int rmq_query_noalloc(const float *d_vals, int64_t n, int64_t bs,
     if (rc) return rc;
     if (dev.device >= kMaxDevices)
         return set_error(RMQ_ENOTSUP, "rmq_query_noalloc: device %d unsupported", dev.device);
-    void *base_v = nullptr;
-    rc = scratch_address(dev.device, &base_v);
+    void *base = nullptr;
+    rc = scratch_address(dev.device, &base);
     if (rc) return rc;
-    char *base = static_cast<char *>(base_v);
-    p.pre = reinterpret_cast<Entry *>(base);
-    p.suf = reinterpret_cast<Entry *>(base + pre_b);
-    p.st = reinterpret_cast<Entry *>(base + 2 * pre_b);
-    p.mst = p.micro ? reinterpret_cast<Entry *>(base + 2 * pre_b + st_b) : nullptr;
-    unsigned long long *invalid =
-        reinterpret_cast<unsigned long long *>(base + 2 * pre_b + st_b + mst_b);
+    unsigned long long *invalid = place_index(p, base);
 
     cudaError_t err = cudaMemsetAsync(invalid, 0, sizeof(unsigned long long), stream);
     if (err == cudaSuccess) err = launch_build(p, dev, stream);

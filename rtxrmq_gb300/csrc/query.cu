@@ -88,6 +88,8 @@ V1View view_of(const BuildPlan &p) {
     v.st = p.st;
     v.mst = p.micro ? p.mst : nullptr;
     v.nmicro = p.micro ? p.nmicro : 0u;
+    v.mpre = p.micro ? p.mpre : nullptr;
+    v.msuf = p.micro ? p.msuf : nullptr;
     return v;
 }
 

@@ -44,6 +44,8 @@ struct V1View {
     // warp-cooperative scan)
     const Entry *mst;
     uint32_t nmicro;
+    const Entry *mpre;  // in-micro-block prefix / suffix minima
+    const Entry *msuf;
 };
 
 // Leftmost minimum of local A[a..b] (b - a < 32, at most 9 float4 loads)
@@ -102,14 +104,15 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
     return e;
 }
 
-// Same-block query through the sub-block level: partial micro-blocks at both
-// ends by one thread each, the micro-blocks between from the micro table.
+// Same-block query through the sub-block level: the partial micro-blocks at
+// both ends from the in-micro-block suffix / prefix minima, the micro-blocks
+// between from the micro table; a query inside one micro-block is one
+// thread's scan of at most 32 values (one 128-byte line).
 template <bool ALIGNED>
 __device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
     const uint32_t ml = l >> 5, mr = r >> 5;
     if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
-    Entry e = better(thread_range_min<ALIGNED>(v, l, ml * 32u + 31u),
-                     thread_range_min<ALIGNED>(v, mr * 32u, r));
+    Entry e = better(v.msuf[l], v.mpre[r]);
     if (mr - ml >= 2u) {
         const uint32_t lo = ml + 1u, hi = mr - 1u;
         const int k = ilog2(hi - lo + 1u);
