@@ -492,6 +492,25 @@ def main():
                 del hQ, hV, hI
             if lr == -1:
                 headline = (name, lr, Q, bs)
+                # energy: NVML board power over ~1.5 s of headline steps (outside
+                # the timed region), as the reference's power CSVs
+                # (scripts/plot_rmq_per_joule.py: q * reps / joules)
+                from rtxrmq_gb300.power import PowerSampler
+                reps_e = max(1, int(1500.0 / max(ms, 1e-3)))
+                torch.cuda.synchronize()
+                with PowerSampler(local, sample_ms=50) as ps:
+                    for _ in range(reps_e):
+                        fn()
+                    torch.cuda.synchronize()
+                if ps.available and ps.energy_joules:
+                    res["energy"] = {"rmq_per_joule": q * reps_e / ps.energy_joules,
+                                     "avg_watts": ps.avg_watts, "seconds": ps.seconds,
+                                     "reps": reps_e, "source": "NVML board power, 50 ms samples",
+                                     "reference": "RTXRMQ on RTX 6000 Ada: 1.20e6 RMQ/J "
+                                                  "(2^26 x 512 queries / 28625.93 J, "
+                                                  "scripts/plot_rmq_per_joule.py:69)"}
+                else:
+                    res["energy"] = {"unavailable": f"NVML status {ps.status}"}
             ix.close()
             results[name] = res
             del dQ
@@ -534,6 +553,7 @@ def main():
                      "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
         "clocks": clocks,
         "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
+        "energy": h.get("energy"),
         "batched": batched,
         "autograd": autograd,
     }

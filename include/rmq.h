@@ -262,6 +262,21 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts,
                        int32_t *h_bucket_bs);
 
 /*
+ * GPU power sampling around a timed region, the role of the reference's
+ * GPUPowerBegin / GPUPowerEnd (common/nvmlPower.cpp:91-167, used around the
+ * timed loop at src/rtx.h:148-158). A thread reads the board power of CUDA
+ * device `device` through NVML every sample_ms and, when `path` is given,
+ * writes the reference's table (#timestep power acc-energy avg-power dt
+ * acc-time). cooldown_ms is slept after starting / before stopping (the
+ * reference uses 1000 ms). NVML is loaded at run time and only read;
+ * RMQ_ENOTSUP when it is not available. One sampler at a time.
+ */
+int rmq_power_begin(int32_t device, int32_t sample_ms, int32_t cooldown_ms,
+                    const char *path);
+int rmq_power_end(int32_t cooldown_ms, double *avg_watts, double *energy_joules,
+                  double *seconds);
+
+/*
  * Host-side synthetic inputs (OpenMP; the output does not depend on the
  * thread count, unlike the reference's per-thread mt19937(seed*tid)
  * streams, src/rand.cuh:120-173).

@@ -73,6 +73,8 @@ SIGNATURES = {
     "rmq_batch_invalid_count": (C.c_int, [_vp, _vp, C.POINTER(_i64)]),
     "rmq_batch_free": (C.c_int, [_vp]),
     "rmq_batch_autotune": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp]),
+    "rmq_power_begin": (C.c_int, [_i32, _i32, _i32, C.c_char_p]),
+    "rmq_power_end": (C.c_int, [_i32, C.POINTER(_dbl), C.POINTER(_dbl), C.POINTER(_dbl)]),
     "rmq_gen_values_uniform": (C.c_int, [_vp, _i64, _u64]),
     "rmq_gen_values_normal": (C.c_int, [_vp, _i64, _dbl, _dbl, _u64]),
     "rmq_gen_values_int": (C.c_int, [_vp, _i64, _i32, _u64]),

@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp"]
 
 LIB_CU = ["api.cu", "build.cu", "query.cu", "batch.cu", "noalloc.cu"]
-LIB_CPP = ["gen.cpp"]
+LIB_CPP = ["gen.cpp", "power.cpp"]
 CLI_CPP = ["cli.cpp"]
 
 
@@ -90,7 +90,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     lib_objs = [obj_dir / (s + ".o") for s in LIB_CU + LIB_CPP]
     if force or _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs),
-              "-Xcompiler", "-fopenmp", "-lgomp"])
+              "-Xcompiler", "-fopenmp", "-lgomp", "-ldl", "-lpthread"])
     cli = OUT / "rtxrmq"
     cli_objs = [obj_dir / (s + ".o") for s in CLI_CPP]
     if force or _stale(cli, cli_objs + [lib]):

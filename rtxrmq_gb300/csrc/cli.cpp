@@ -72,7 +72,7 @@ void usage() {
                  "   --seed <seed>             seed for PRNG\n"
                  "   --check                   check correctness against GPU BASE\n"
                  "   --save-time=<file>        append a CSV row\n"
-                 "   --save-power=<file>       (not available in this engine)\n",
+                 "   --save-power=<file>       sample GPU power (NVML) around the timed loop\n",
                  kAlgStr[2], kAlgStr[5]);
 }
 
@@ -214,8 +214,6 @@ int main(int argc, char **argv) {
                      a.alg);
         return 2;
     }
-    if (a.save_power)
-        std::fprintf(stderr, "warning: --save-power is not available in this engine; ignored\n");
 
     CK(cudaSetDevice(a.dev));
     cudaDeviceProp prop;
@@ -271,6 +269,19 @@ int main(int argc, char **argv) {
     std::printf("Computing RMQs%s (%-16s,r=%-3i)...", idx_mode ? " index" : "", alg_name(a.alg),
                 a.reps);
     std::fflush(stdout);
+    bool sampling = false;
+    if (a.save_power) {
+        // src/rtx.h:148-158: 100 ms samples around the timed loop, the
+        // reference's file name when none is given
+        const std::string f = a.power_file.empty()
+                                  ? std::string("../results/power-") + alg_name(a.alg) + ".dat"
+                                  : a.power_file;
+        const int prc = rmq_power_begin(a.dev, 100, 1000, f.c_str());
+        if (prc == RMQ_OK)
+            sampling = true;
+        else
+            std::fprintf(stderr, "warning: power sampling unavailable (status %d); continuing\n", prc);
+    }
     t0 = std::chrono::steady_clock::now();
     for (int i = 0; i < a.reps; ++i) {
         if (base_alg == 5)
@@ -280,6 +291,13 @@ int main(int argc, char **argv) {
         CK(cudaDeviceSynchronize());
     }
     const double timems = ms_since(t0);
+    if (sampling) {
+        double watts = 0, joules = 0, secs = 0;
+        if (rmq_power_end(1000, &watts, &joules, &secs) == RMQ_OK)
+            std::printf("power: %.2f W average, %.2f J over %.2f s sampled [%.3e RMQs/J]\n", watts,
+                        joules, secs,
+                        joules > 0 ? static_cast<double>(a.q) * a.reps / joules : 0.0);
+    }
     const double avg = timems / (1000.0 * a.reps);
     std::printf("done: %f secs (avg %f secs): [%.2f RMQs/sec, %f nsec/RMQ]\n", timems / 1000.0, avg,
                 static_cast<double>(a.q) / avg, avg * 1e9 / static_cast<double>(a.q));

@@ -191,3 +191,43 @@ def test_ragged_workload_shapes(native):
     d = W.differentiable_rows(nrows=8, lmin=1000, lmax=2000, q_per_row=100, seed=4)
     assert d.span == int(d.lengths.sum()) and (d.qcounts == 100).all()
     assert abs(float(d.values.mean())) < 0.1
+
+
+FAKE_NVML = r"""
+int nvmlInit_v2(void) { return 0; }
+int nvmlShutdown(void) { return 0; }
+int nvmlDeviceGetHandleByIndex_v2(unsigned i, void **d) { *d = (void *)0x1234; return i == 0 ? 0 : 2; }
+int nvmlDeviceGetHandleByPciBusId_v2(const char *b, void **d) { *d = (void *)0x1234; return 0; }
+int nvmlDeviceGetPowerUsage(void *d, unsigned *mw) { *mw = 250000u; return d == (void *)0x1234 ? 0 : 1; }
+"""
+
+
+def test_power_sampler_against_fake_nvml(native, tmp_path, monkeypatch):
+    """rmq_power_begin / end (the role of GPUPowerBegin / GPUPowerEnd,
+    common/nvmlPower.cpp) against a fake NVML that reports 250 W: the table
+    has the reference's columns, energy integrates power over time."""
+    import time
+
+    from rtxrmq_gb300.power import PowerSampler
+    src = tmp_path / "fake_nvml.c"
+    src.write_text(FAKE_NVML)
+    so = tmp_path / "libfake_nvml.so"
+    r = subprocess.run(["gcc", "-shared", "-fPIC", "-o", str(so), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    monkeypatch.setenv("RTXRMQ_NVML_LIBRARY", str(so))
+    table = tmp_path / "power.dat"
+    with PowerSampler(0, sample_ms=20, path=str(table)) as p:
+        assert p.available
+        assert native.rmq_power_begin(0, 20, 0, None) == -1  # one sampler at a time
+        time.sleep(0.3)
+    assert abs(p.avg_watts - 250.0) < 1e-9
+    assert abs(p.energy_joules - 250.0 * p.seconds) < 1e-6 and 0.2 < p.seconds < 1.0
+    lines = table.read_text().splitlines()
+    assert lines[0].split() == ["#timestep", "power", "acc-energy", "avg-power", "dt", "acc-time"]
+    rows = [list(map(float, ln.split())) for ln in lines[1:]]
+    assert len(rows) >= 5 and all(row[1] == 250.0 for row in rows)
+    assert abs(rows[-1][2] - p.energy_joules) < 1e-3
+    assert native.rmq_power_end(0, None, None, None) == -1  # not running
+    monkeypatch.setenv("RTXRMQ_NVML_LIBRARY", str(tmp_path / "missing.so"))
+    with PowerSampler(0) as q:
+        assert not q.available and q.status == -5
