@@ -11,8 +11,8 @@ of each mode is the fastest of a sweep over 2^10..2^16.
 value      -- RMQ/s of the device-resident step (inputs already in HBM),
               timed with CUDA events on the launching stream.
 e2e        -- the same step through the C ABI with host buffers
-              (rmq_query_host): the kernel reads the pinned host queries and
-              writes values + indices into pinned host memory over
+              (rmq_query_host): the query kernel reads the pinned host queries
+              and writes values + indices into pinned host memory over
               NVLink-C2C, all inside the timed region.
 roofline   -- algorithmic HBM bytes per launch (query read + result write +
               one 32-byte sector per pre/suf lookup, 32 bytes per sector a
@@ -487,7 +487,7 @@ def main():
                 res["e2e"] = {"value": world * q / (e2e_ms / 1e3), "unit": "RMQ/s",
                               "h2d_bytes_per_step": int(Q.nbytes),
                               "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
-                              "ms_per_step": e2e_ms, "path": "rmq_query_host, pinned host buffers",
+                              "ms_per_step": e2e_ms, "path": "rmq_query_host, pinned host buffers read and written in place",
                               "matches_device_path": bool(ok)}
                 del hQ, hV, hI
             if lr == -1:

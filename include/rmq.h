@@ -111,17 +111,20 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
               float *d_val, int32_t *d_idx, rmq_stream_t stream);
 
 /*
- * rmq_query with host-side buffers: h_queries, h_val, h_idx live in host
- * memory that the GPU can address -- page-locked memory (cudaHostAlloc,
- * cudaHostRegister) or, on systems where the device reads pageable memory
- * (Grace-Blackwell: cudaDevAttrPageableMemoryAccess), any host memory; device
- * pointers are accepted as well. The query kernel reads the queries and
- * writes the results in place over the host link (NVLink-C2C on GB300), so
- * no staging copies are made and nothing is allocated. Stream ordered: the
- * results are in the host buffers once `stream` has been synchronised.
- * A buffer the device cannot address is rejected with RMQ_EINVAL.
- * This is the end-to-end form of the reference's timed loop plus its
- * copy-out (src/rtx.h:150-159).
+ * rmq_query with host-side buffers (h_queries, h_val, h_idx in host memory;
+ * device pointers are used as they are). When the GPU can address every
+ * buffer -- page-locked memory (cudaHostAlloc, cudaHostRegister), or any
+ * host memory on systems where the device reads pageable memory
+ * (Grace-Blackwell) -- the query kernel reads the queries and writes the
+ * results in place over the host link (NVLink-C2C on GB300), with no staging
+ * copies and no allocation. Otherwise the work is staged through device
+ * memory in 4 Mi-query chunks on two internal streams (queries copied in or
+ * read in place, results copied out while later chunks run); that path
+ * allocates its staging (192 MB) and streams on its first call on a handle.
+ * Stream ordered with respect to `stream`: the results are in the host
+ * buffers once `stream` has been synchronised. Calls on one handle from
+ * several threads are serialised on the staged path. This is the end-to-end
+ * form of the reference's timed loop plus its copy-out (src/rtx.h:150-159).
  */
 int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q,
                    float *h_val, int32_t *h_idx, rmq_stream_t stream);

@@ -108,9 +108,9 @@ class RMQIndex:
 
     def query_host(self, queries, out_val=None, out_idx=None, stream=None) -> None:
         """rmq_query_host: host-side buffers (CPU tensors or numpy arrays;
-        page-locked memory, or any memory where the device reads pageable
-        memory) read and written in place by the kernel. Results are valid
-        after the stream is synchronised."""
+        page-locked ones make the copies asynchronous), streamed through
+        device staging in chunks that overlap copies and queries. Results are
+        valid after the stream is synchronised."""
         def hptr(x):
             if x is None:
                 return None

@@ -7,6 +7,7 @@
 // plus a per-thread message.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -20,7 +21,24 @@ struct rmq_handle {
     size_t mem_bytes;
     unsigned long long *invalid;    // device counter of rejected queries
     int64_t table_bytes;
+    // rmq_query_host pipeline, created on its first call: device staging for
+    // kHostStreams chunks (queries in, values and indices out), its streams
+    // and events, and a lock that keeps concurrent calls from interleaving
+    // their chunks on the shared staging buffers
+    std::mutex *host_mu;
+    void *stage;
+    cudaStream_t ks;           // chunk kernels (and query copies), in order
+    cudaStream_t cs;           // result copies, each after its chunk's kernel
+    cudaEvent_t ev_start;
+    cudaEvent_t k_done[3];     // per staging slot: kernel finished
+    cudaEvent_t c_done[3];     // per staging slot: results copied out
+    cudaEvent_t ev_end;
 };
+
+namespace {
+constexpr int kHostStreams = 3;
+constexpr int64_t kHostChunk = int64_t(1) << 22;  // queries per staged chunk (64 MB of staging)
+}  // namespace
 
 namespace rmq {
 
@@ -121,9 +139,15 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     rmq_handle_t *h = new (std::nothrow) rmq_handle_t;
     if (!h) return set_error(RMQ_ENOMEM, "rmq_build: host allocation failed");
     std::memset(h, 0, sizeof(*h));
+    h->host_mu = new (std::nothrow) std::mutex;
+    if (!h->host_mu) {
+        delete h;
+        return set_error(RMQ_ENOMEM, "rmq_build: host allocation failed");
+    }
     h->device = dev.device;
     cudaError_t err = cudaMalloc(&h->mem, total);
     if (err != cudaSuccess) {
+        delete h->host_mu;
         delete h;
         cudaGetLastError();
         return set_error(RMQ_ENOMEM, "rmq_build: cudaMalloc(%zu bytes) failed: %s", total,
@@ -139,6 +163,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     if (err != cudaSuccess) {
         rc = cuda_fail(err, "rmq_build: launch");
         cudaFree(h->mem);
+        delete h->host_mu;
         delete h;
         return rc;
     }
@@ -176,35 +201,32 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float 
     return RMQ_OK;
 }
 
-// Device-usable address of a buffer the caller calls "host" memory, or null
-// if the current device cannot address it.
-static const void *device_view(const void *p, bool *ok) {
-    *ok = false;
-    if (!p) {
-        *ok = true;
-        return nullptr;
-    }
+// True when p is device (or managed) memory of the current context.
+static bool is_device_memory(const void *p) {
     cudaPointerAttributes at;
-    cudaError_t err = cudaPointerGetAttributes(&at, p);
-    if (err != cudaSuccess) {
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Device-usable address of host memory the GPU can read in place
+// (page-locked and mapped, or any memory where the device reads pageable
+// memory), or null.
+static const void *device_address(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
-        *ok = true;
-        return p;
-    }
-    if (at.type == cudaMemoryTypeHost && at.devicePointer) {
-        *ok = true;
-        return at.devicePointer;
-    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) return at.devicePointer;
     int dev = 0, pageable = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
-        pageable) {
-        *ok = true;
+        pageable)
         return p;
-    }
     cudaGetLastError();
     return nullptr;
 }
@@ -217,22 +239,122 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
     if (q == 0) return RMQ_OK;
     if (!h_queries) return set_error(RMQ_EINVAL, "rmq_query_host: h_queries is NULL");
     if (!h_val && !h_idx) return set_error(RMQ_EINVAL, "rmq_query_host: both outputs are NULL");
-    bool okq, okv, oki;
-    const void *dq = device_view(h_queries, &okq);
-    void *dv = const_cast<void *>(device_view(h_val, &okv));
-    void *di = const_cast<void *>(device_view(h_idx, &oki));
-    if (!okq || !okv || !oki)
-        return set_error(RMQ_EINVAL,
-                         "rmq_query_host: a buffer is not addressable by the device "
-                         "(page-lock it with cudaHostRegister or allocate it with cudaHostAlloc)");
-    return rmq_query(h, static_cast<const int32_t *>(dq), q, static_cast<float *>(dv),
-                     static_cast<int32_t *>(di), stream);
+    // RTXRMQ_HOST_STAGED=1 takes the staged path even for addressable
+    // buffers (it is otherwise only reached on systems without page-locked
+    // or pageable access; the tests use it to cover that path everywhere)
+    const char *force = std::getenv("RTXRMQ_HOST_STAGED");
+    const bool forced = force && force[0] == '1';
+    if (!forced) {
+        // every buffer addressable by the device (device memory, page-locked
+        // host memory, or host memory on a system where the device reads
+        // pageable memory): the query kernel reads and writes them in place
+        const void *dq = device_address(h_queries);
+        const void *dv = h_val ? device_address(h_val) : nullptr;
+        const void *di = h_idx ? device_address(h_idx) : nullptr;
+        if (dq && (!h_val || dv) && (!h_idx || di))
+            return rmq_query(h, static_cast<const int32_t *>(dq), q,
+                             static_cast<float *>(const_cast<void *>(dv)),
+                             static_cast<int32_t *>(const_cast<void *>(di)), stream);
+    }
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    if (dev.device != h->device)
+        return set_error(RMQ_EINVAL, "rmq_query_host: handle built on device %d, current is %d",
+                         h->device, dev.device);
+    rmq_handle_t *hm = const_cast<rmq_handle_t *>(h);
+    std::lock_guard<std::mutex> lock(*hm->host_mu);
+    cudaError_t err = cudaSuccess;
+    if (!hm->stage) {
+        err = cudaMalloc(&hm->stage, kHostStreams * kHostChunk * 16);
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->ks, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->cs, cudaStreamNonBlocking);
+        for (int s = 0; s < kHostStreams && err == cudaSuccess; ++s) {
+            err = cudaEventCreateWithFlags(&hm->k_done[s], cudaEventDisableTiming);
+            if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->c_done[s], cudaEventDisableTiming);
+        }
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->ev_start, cudaEventDisableTiming);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->ev_end, cudaEventDisableTiming);
+        if (err != cudaSuccess) return cuda_fail(err, "rmq_query_host: staging set-up");
+    }
+    err = cudaEventRecord(hm->ev_start, stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->ks, hm->ev_start, 0);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->cs, hm->ev_start, 0);
+    // Queries the device can address are read in place by the kernel (on
+    // Grace-Blackwell at no cost to the kernel); others are copied into
+    // staging. Results go to device staging and are copied out by the copy
+    // engines (kernel stores into host memory slow the kernel's lookups).
+    // The chunk kernels run in order on one stream; each chunk's result copy
+    // follows on a second stream, overlapping the next chunks' kernels; a
+    // staging slot is reused only after its previous copy-out finished.
+    const int2 *qdev = forced ? nullptr : static_cast<const int2 *>(device_address(h_queries));
+    const bool val_dev = h_val && is_device_memory(h_val);
+    const bool idx_dev = h_idx && is_device_memory(h_idx);
+    for (int64_t c = 0, i = 0; c < q && err == cudaSuccess; c += kHostChunk, ++i) {
+        const int b = static_cast<int>(i % kHostStreams);
+        const int64_t m = q - c < kHostChunk ? q - c : kHostChunk;
+        char *base = static_cast<char *>(hm->stage) + b * kHostChunk * 16;
+        if (i >= kHostStreams) err = cudaStreamWaitEvent(hm->ks, hm->c_done[b], 0);
+        if (err != cudaSuccess) break;
+        QueryArgs a;
+        if (qdev) {
+            a.Q = qdev + c;
+        } else {
+            int32_t *dq = reinterpret_cast<int32_t *>(base);
+            err = cudaMemcpyAsync(dq, h_queries + 2 * c, m * 8, cudaMemcpyHostToDevice, hm->ks);
+            if (err != cudaSuccess) break;
+            a.Q = reinterpret_cast<const int2 *>(dq);
+        }
+        float *dv = !h_val ? nullptr
+                    : val_dev ? h_val + c : reinterpret_cast<float *>(base + kHostChunk * 8);
+        int32_t *di = !h_idx ? nullptr
+                      : idx_dev ? h_idx + c : reinterpret_cast<int32_t *>(base + kHostChunk * 12);
+        a.q = m;
+        a.val = dv;
+        a.idx = di;
+        a.invalid = h->invalid;
+        err = launch_query(h->plan, a, dev, hm->ks);
+        if (err == cudaSuccess) err = cudaEventRecord(hm->k_done[b], hm->ks);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->cs, hm->k_done[b], 0);
+        if (err == cudaSuccess && h_val && !val_dev)
+            err = cudaMemcpyAsync(h_val + c, dv, m * 4, cudaMemcpyDeviceToHost, hm->cs);
+        if (err == cudaSuccess && h_idx && !idx_dev)
+            err = cudaMemcpyAsync(h_idx + c, di, m * 4, cudaMemcpyDeviceToHost, hm->cs);
+        if (err == cudaSuccess) err = cudaEventRecord(hm->c_done[b], hm->cs);
+    }
+    // `stream` continues when both internal streams are done
+    if (err == cudaSuccess) err = cudaEventRecord(hm->ev_end, hm->ks);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(stream, hm->ev_end, 0);
+    if (err == cudaSuccess) err = cudaEventRecord(hm->ev_end, hm->cs);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(stream, hm->ev_end, 0);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_query_host");
+    return RMQ_OK;
 }
 
 int rmq_free(rmq_handle_t *h) {
     g_err[0] = '\0';
     if (!h) return RMQ_OK;
-    cudaError_t err = cudaFree(h->mem);
+    cudaError_t err = cudaSuccess;
+    if (h->stage) {
+        if (h->ks) {
+            cudaStreamSynchronize(h->ks);
+            cudaStreamDestroy(h->ks);
+        }
+        if (h->cs) {
+            cudaStreamSynchronize(h->cs);
+            cudaStreamDestroy(h->cs);
+        }
+        for (int s = 0; s < kHostStreams; ++s) {
+            if (h->k_done[s]) cudaEventDestroy(h->k_done[s]);
+            if (h->c_done[s]) cudaEventDestroy(h->c_done[s]);
+        }
+        if (h->ev_start) cudaEventDestroy(h->ev_start);
+        if (h->ev_end) cudaEventDestroy(h->ev_end);
+        err = cudaFree(h->stage);
+    }
+    cudaError_t e2 = cudaFree(h->mem);
+    if (err == cudaSuccess) err = e2;
+    delete h->host_mu;
     delete h;
     if (err != cudaSuccess) return cuda_fail(err, "rmq_free: cudaFree");
     return RMQ_OK;

@@ -16,15 +16,32 @@ namespace rmq {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kQPT = 2;
+#ifndef RMQ_QUERY_QPT
+#define RMQ_QUERY_QPT 2  // queries per thread per step (independent lookups in flight)
+#endif
+constexpr int kQPT = RMQ_QUERY_QPT;
 
+// Grid-stride over steps of 256 * kQPT queries; the next step's queries are
+// loaded before the current step is answered, so their latency (host memory
+// over the host link when called through rmq_query_host) overlaps the
+// current step's lookups.
 template <bool ALIGNED>
 __global__ void __launch_bounds__(kThreads)
 query_kernel(V1View v, QueryOut o, int64_t q) {
     const int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
-    for (int64_t c0 = static_cast<int64_t>(blockIdx.x) * chunk; c0 < q;
-         c0 += static_cast<int64_t>(gridDim.x) * chunk)
-        answer_range<ALIGNED, kQPT>(v, o, c0, c0 + chunk < q ? c0 + chunk : q);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * chunk;
+    int64_t c0 = static_cast<int64_t>(blockIdx.x) * chunk;
+    if (c0 >= q) return;
+    int2 cur[kQPT];
+    load_queries<kQPT>(o, c0, c0 + chunk < q ? c0 + chunk : q, cur);
+    for (; c0 < q; c0 += stride) {
+        const int64_t c1 = c0 + stride;
+        int2 nxt[kQPT];
+        if (c1 < q) load_queries<kQPT>(o, c1, c1 + chunk < q ? c1 + chunk : q, nxt);
+        answer_step<ALIGNED, kQPT>(v, o, c0, c0 + chunk < q ? c0 + chunk : q, cur);
+#pragma unroll
+        for (int k = 0; k < kQPT; ++k) cur[k] = nxt[k];
+    }
 }
 
 __global__ void __launch_bounds__(kThreads)

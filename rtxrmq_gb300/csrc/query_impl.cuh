@@ -192,12 +192,29 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
 // uniform across the CTA (warp-cooperative scans need full warps).
 // QPT queries per thread per iteration keep several independent lookups in
 // flight per thread.
+// Queries base + threadIdx.x + k * blockDim.x (k < QPT) of [.., q1), loaded
+// ahead of use (the query stream may come from host memory over the host
+// link, so a caller can issue the next step's loads before answering the
+// current step).
+template <int QPT>
+__device__ __forceinline__ void load_queries(const QueryOut &o, int64_t base, int64_t q1,
+                                             int2 (&qq)[QPT]) {
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+        const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
+        qq[k] = make_int2(0, 0);
+        if (i < q1) qq[k] = __ldcs(o.Q + i);
+    }
+}
+
+// One step of the CTA: the QPT * blockDim.x queries starting at `base`,
+// already loaded into qq. Uniform across the CTA (warp-cooperative scans
+// need full warps).
 template <bool ALIGNED, int QPT>
-__device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o, int64_t q0,
-                                             int64_t q1) {
+__device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, int64_t base,
+                                            int64_t q1, const int2 (&qq)[QPT]) {
     const int lane = threadIdx.x & 31;
-    const int64_t step = static_cast<int64_t>(blockDim.x) * QPT;
-    for (int64_t base = q0; base < q1; base += step) {
+    {
         uint32_t l[QPT], r[QPT];
         bool act[QPT], ok[QPT], scan[QPT];
         Entry es[QPT], ep[QPT], ea[QPT], eb[QPT];
@@ -205,11 +222,10 @@ __device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o,
         for (int k = 0; k < QPT; ++k) {
             const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
             act[k] = i < q1;
-            int2 qq = make_int2(0, 0);
-            if (act[k]) qq = __ldcs(o.Q + i);
-            ok[k] = act[k] && qq.x >= 0 && qq.x <= qq.y && static_cast<uint32_t>(qq.y) < v.n;
-            l[k] = ok[k] ? static_cast<uint32_t>(qq.x) : 0u;
-            r[k] = ok[k] ? static_cast<uint32_t>(qq.y) : 0u;
+            ok[k] = act[k] && qq[k].x >= 0 && qq[k].x <= qq[k].y &&
+                    static_cast<uint32_t>(qq[k].y) < v.n;
+            l[k] = ok[k] ? static_cast<uint32_t>(qq[k].x) : 0u;
+            r[k] = ok[k] ? static_cast<uint32_t>(qq[k].y) : 0u;
         }
 #pragma unroll
         for (int k = 0; k < QPT; ++k) {
@@ -234,6 +250,25 @@ __device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o,
                 eb[k] = lvl[hi + 1u - (1u << lev)];
             }
         }
+        if (v.mst) {
+            // sub-block level: every query of the step is answered by its own
+            // thread, so each result is stored once and a warp's 128-byte output
+            // line is written by one instruction (partial-line writes cost
+            // extra transactions, most of all to host memory)
+#pragma unroll
+            for (int k = 0; k < QPT; ++k) {
+                if (!act[k]) continue;
+                const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
+                if (!ok[k]) {
+                    put_invalid(o, i);
+                    continue;
+                }
+                const Entry e = scan[k] ? micro_query<ALIGNED>(v, l[k], r[k])
+                                        : better(better(es[k], ep[k]), better(ea[k], eb[k]));
+                put_result(o, i, e);
+            }
+            return;
+        }
 #pragma unroll
         for (int k = 0; k < QPT; ++k) {
             if (act[k] && !scan[k]) {
@@ -243,14 +278,6 @@ __device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o,
                 else
                     put_invalid(o, i);
             }
-        }
-        if (v.mst) {
-#pragma unroll
-            for (int k = 0; k < QPT; ++k)
-                if (scan[k])
-                    put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x,
-                               micro_query<ALIGNED>(v, l[k], r[k]));
-            continue;
         }
 #pragma unroll
         for (int k = 0; k < QPT; ++k) {
@@ -265,6 +292,19 @@ __device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o,
                     put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e);
             }
         }
+    }
+}
+
+// Answer queries [q0, q1) of one array with the whole CTA, QPT queries per
+// thread per step.
+template <bool ALIGNED, int QPT>
+__device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o, int64_t q0,
+                                             int64_t q1) {
+    const int64_t step = static_cast<int64_t>(blockDim.x) * QPT;
+    for (int64_t base = q0; base < q1; base += step) {
+        int2 qq[QPT];
+        load_queries<QPT>(o, base, q1, qq);
+        answer_step<ALIGNED, QPT>(v, o, base, q1, qq);
     }
 }
 

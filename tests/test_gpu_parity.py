@@ -236,9 +236,9 @@ def test_cli_check_passes(native):
 
 
 def test_query_host_buffers(cuda, native, oracle_lib):
-    """rmq_query_host: pinned host buffers are read and written in place;
-    pageable buffers are served in place where the device reads pageable
-    memory, and rejected with RMQ_EINVAL elsewhere."""
+    """rmq_query_host: pinned and pageable host buffers, streamed through the
+    staged pipeline (several chunks: q > one 4 Mi-query chunk is exercised by
+    the full-size bench); device buffers are passed through."""
     import torch
 
     import rtxrmq_gb300 as R
@@ -259,11 +259,62 @@ def test_query_host_buffers(cuda, native, oracle_lib):
         np.testing.assert_array_equal(hI.numpy(), ei)
         v = np.full(q, np.nan, np.float32)
         i = np.full(q, -7, np.int32)
-        try:
-            ix.query_host(Q, v, i)
+        ix.query_host(Q, v, i)  # pageable numpy buffers
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(i, ei)
+        np.testing.assert_array_equal(bits(v), bits(ev))
+        dv = torch.empty(q, dtype=torch.float32, device=cuda)
+        di = torch.empty(q, dtype=torch.int32, device=cuda)
+        ix.query_host(torch.from_numpy(Q).to(cuda), dv, di)  # device buffers pass through
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(di.cpu().numpy(), ei)
+
+
+def test_query_host_many_chunks(cuda, native, oracle_lib):
+    """More queries than three staging chunks (4 Mi queries each), values
+    only and indices only, against the device path."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n, q = 1 << 22, (3 << 22) + 12345
+    A = R.gen_values_int(n, 5000, 21)
+    Q = R.gen_queries(q, n, -3, 21)
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), 4096) as ix:
+        dv, di = ix.query(torch.from_numpy(Q).to(cuda))
+        hQ = torch.from_numpy(Q).pin_memory()
+        hv = torch.empty(q, dtype=torch.float32).pin_memory()
+        hi = torch.empty(q, dtype=torch.int32).pin_memory()
+        ix.query_host(hQ, hv, hi)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(hi.numpy(), di.cpu().numpy())
+        np.testing.assert_array_equal(bits(hv.numpy()), bits(dv.cpu().numpy()))
+        hi2 = torch.full((q,), -9, dtype=torch.int32).pin_memory()
+        ix.query_host(hQ, None, hi2)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(hi2.numpy(), di.cpu().numpy())
+
+
+def test_query_host_staged_path(cuda, native, oracle_lib, monkeypatch):
+    """The staged host path (device staging, query copies or in-place reads,
+    result copies overlapping later chunks) gives the same results; forced
+    with RTXRMQ_HOST_STAGED=1 because buffers here are addressable."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    monkeypatch.setenv("RTXRMQ_HOST_STAGED", "1")
+    n, q = 1 << 21, (1 << 23) + 777  # three chunks
+    A = R.gen_values_int(n, 3000, 31)
+    Q = R.gen_queries(q, n, -3, 31)
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), 2048) as ix:
+        dv, di = ix.query(torch.from_numpy(Q).to(cuda))
+        dv, di = dv.cpu().numpy(), di.cpu().numpy()
+        for pinned in (True, False):
+            hQ = torch.from_numpy(Q)
+            hv = torch.empty(q, dtype=torch.float32)
+            hi = torch.empty(q, dtype=torch.int32)
+            if pinned:
+                hQ, hv, hi = hQ.pin_memory(), hv.pin_memory(), hi.pin_memory()
+            ix.query_host(hQ, hv, hi)
             torch.cuda.synchronize()
-        except R.RMQError as e:
-            assert e.code == -1 and "addressable" in str(e)
-        else:
-            np.testing.assert_array_equal(i, ei)
-            np.testing.assert_array_equal(bits(v), bits(ev))
+            np.testing.assert_array_equal(hi.numpy(), di)
+            np.testing.assert_array_equal(bits(hv.numpy()), bits(dv))
