@@ -149,6 +149,20 @@ int rmq_query_noalloc(const float *d_vals, int64_t n, int64_t bs,
                       const int32_t *d_queries, int64_t q, float *d_val,
                       int32_t *d_idx, rmq_stream_t stream);
 
+/*
+ * Persisted index, the role of HRMQ's saveDS / loadDS
+ * (hrmq/RMQRMM64.cpp:1471-1659). rmq_save writes a header (layout sizes and
+ * a 64-bit fingerprint of all the values, computed on the GPU) and the
+ * handle's device structure to `path`; the values themselves are not stored.
+ * rmq_load recreates the handle for d_vals[0..n), which must be the values
+ * the index was built from: a different length, layout or fingerprint, a
+ * truncated or foreign file give RMQ_EINVAL. Both synchronise `stream` and
+ * use a temporary device word for the fingerprint.
+ */
+int rmq_save(const rmq_handle_t *h, const char *path, rmq_stream_t stream);
+int rmq_load(const float *d_vals, int64_t n, const char *path,
+             rmq_stream_t stream, rmq_handle_t **out);
+
 /* Release everything the handle owns. NULL is accepted. */
 int rmq_free(rmq_handle_t *h);
 

@@ -107,10 +107,11 @@ class RMQIndex:
         return out_val, out_idx
 
     def query_host(self, queries, out_val=None, out_idx=None, stream=None) -> None:
-        """rmq_query_host: host-side buffers (CPU tensors or numpy arrays;
-        page-locked ones make the copies asynchronous), streamed through
-        device staging in chunks that overlap copies and queries. Results are
-        valid after the stream is synchronised."""
+        """rmq_query_host: host-side buffers (CPU tensors or numpy arrays).
+        Buffers the GPU can address (page-locked, or any memory on
+        Grace-Blackwell) are read and written in place by the query kernel;
+        others go through device staging. Results are valid after the stream
+        is synchronised."""
         def hptr(x):
             if x is None:
                 return None
@@ -126,6 +127,24 @@ class RMQIndex:
             raise ValueError("queries must have shape [q, 2]")
         check(load().rmq_query_host(self._h, hptr(queries), q, hptr(out_val), hptr(out_idx),
                                     _stream_handle(stream)))
+
+    def save(self, path, stream=None) -> None:
+        """Write the index (not the values) to ``path`` (rmq_save)."""
+        check(load().rmq_save(self._h, str(path).encode(), _stream_handle(stream)))
+
+    @classmethod
+    def load(cls, values, path, stream=None) -> "RMQIndex":
+        """Index for ``values`` read from ``path`` (rmq_load); the values must
+        be the ones the index was built from."""
+        import torch
+        if values.dtype != torch.float32 or values.dim() != 1:
+            raise TypeError("values must be a 1-D float32 CUDA tensor")
+        self = cls.__new__(cls)
+        self._values = values
+        self._h = C.c_void_p()
+        check(load().rmq_load(_dptr(values), values.numel(), str(path).encode(),
+                              _stream_handle(stream), C.byref(self._h)))
+        return self
 
     def invalid_count(self, stream=None) -> int:
         v = C.c_int64()

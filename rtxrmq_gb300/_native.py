@@ -59,6 +59,8 @@ SIGNATURES = {
     "rmq_query_host": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "rmq_query_noalloc": (C.c_int, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_free": (C.c_int, [_vp]),
+    "rmq_save": (C.c_int, [_vp, C.c_char_p, _vp]),
+    "rmq_load": (C.c_int, [_vp, _i64, C.c_char_p, _vp, C.POINTER(_vp)]),
     "rmq_info": (C.c_int, [_vp, C.POINTER(rmq_info_t)]),
     "rmq_invalid_count": (C.c_int, [_vp, _vp, C.POINTER(_i64)]),
     "rmq_last_error_string": (C.c_char_p, []),

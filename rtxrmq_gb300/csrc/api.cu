@@ -83,11 +83,49 @@ int device_info(DeviceInfo *out) {
     return RMQ_OK;
 }
 
-static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
 }  // namespace rmq
 
 using namespace rmq;
+
+namespace rmq {
+
+int handle_view(const rmq_handle *h, BuildPlan *plan, void **mem, size_t *bytes) {
+    if (!h) return set_error(RMQ_EINVAL, "handle is NULL");
+    *plan = h->plan;
+    *mem = h->mem;
+    *bytes = h->mem_bytes;
+    return RMQ_OK;
+}
+
+int handle_adopt(BuildPlan plan, void *mem, size_t bytes, cudaStream_t stream, rmq_handle **out) {
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    rmq_handle_t *h = new (std::nothrow) rmq_handle_t;
+    if (!h) return set_error(RMQ_ENOMEM, "host allocation failed");
+    std::memset(h, 0, sizeof(*h));
+    h->host_mu = new (std::nothrow) std::mutex;
+    if (!h->host_mu) {
+        delete h;
+        return set_error(RMQ_ENOMEM, "host allocation failed");
+    }
+    h->device = dev.device;
+    h->mem = mem;
+    h->mem_bytes = bytes;
+    h->invalid = place_index(plan, mem);
+    h->table_bytes = static_cast<int64_t>(sizeof(Entry) * static_cast<size_t>(plan.nb) * plan.levels);
+    h->plan = plan;
+    cudaError_t err = cudaMemsetAsync(h->invalid, 0, sizeof(unsigned long long), stream);
+    if (err != cudaSuccess) {
+        delete h->host_mu;
+        delete h;
+        return cuda_fail(err, "clear counter");
+    }
+    *out = h;
+    return RMQ_OK;
+}
+
+}  // namespace rmq
 
 extern "C" {
 

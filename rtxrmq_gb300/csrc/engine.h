@@ -57,6 +57,16 @@ unsigned long long *place_index(BuildPlan &p, void *base);
 uint32_t st_levels(uint32_t nb);
 cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s);
 
+// ---- handles (api.cu) ----
+}  // namespace rmq
+struct rmq_handle;
+namespace rmq {
+// The plan (with its device pointers), allocation and size of a handle.
+int handle_view(const rmq_handle *h, BuildPlan *plan, void **mem, size_t *bytes);
+// A new handle owning `mem` (laid out by place_index for `plan`), with its
+// invalid-query counter cleared on `stream`.
+int handle_adopt(BuildPlan plan, void *mem, size_t bytes, cudaStream_t stream, rmq_handle **out);
+
 // ---- queries (query.cu) ----
 struct QueryArgs {
     const int2 *Q;

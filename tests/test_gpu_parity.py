@@ -318,3 +318,46 @@ def test_query_host_staged_path(cuda, native, oracle_lib, monkeypatch):
             torch.cuda.synchronize()
             np.testing.assert_array_equal(hi.numpy(), di)
             np.testing.assert_array_equal(bits(hv.numpy()), bits(dv))
+
+
+def test_save_load_index(cuda, native, oracle_lib, tmp_path):
+    """rmq_save / rmq_load (the role of HRMQ's saveDS / loadDS): a loaded
+    index answers like the built one; other values, lengths, foreign or
+    truncated files are refused."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = 300_001
+    A = R.gen_values_int(n, 999, 41)
+    Q = np.concatenate([R.gen_queries(50_000, n, L, 41) for L in (-1, -3, 1, 40)])
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
+    for bs, micro in ((1024, True), (1024, False), (1000, True), (1, True)):
+        path = tmp_path / f"ix_{bs}_{micro}.rmq"
+        with R.RMQIndex(dA, bs, micro=micro) as ix:
+            ix.save(path)
+            info = ix.info()
+        with R.RMQIndex.load(dA, path) as ix2:
+            assert ix2.info()["struct_bytes"] == info["struct_bytes"]
+            assert ix2.info()["micro_levels"] == info["micro_levels"]
+            v, i = ix2.query(dQ)
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(i.cpu().numpy(), ei)
+            np.testing.assert_array_equal(bits(v.cpu().numpy()), bits(ev))
+    path = tmp_path / "ix_1024_True.rmq"
+    B = A.copy()
+    B[12345] += 1.0
+    with pytest.raises(R.RMQError, match="values differ"):
+        R.RMQIndex.load(torch.from_numpy(B).to(cuda), path)
+    with pytest.raises(R.RMQError, match="n="):
+        R.RMQIndex.load(dA[:-1].contiguous(), path)
+    raw = path.read_bytes()
+    (tmp_path / "trunc.rmq").write_bytes(raw[:len(raw) // 2])
+    with pytest.raises(R.RMQError, match="truncated"):
+        R.RMQIndex.load(dA, tmp_path / "trunc.rmq")
+    bad = bytearray(raw)
+    bad[20] ^= 0xFF
+    (tmp_path / "bad.rmq").write_bytes(bytes(bad))
+    with pytest.raises(R.RMQError, match="not an index file"):
+        R.RMQIndex.load(dA, tmp_path / "bad.rmq")
