@@ -60,11 +60,21 @@ typedef struct rmq_info {
     int32_t micro_levels; /* levels of the sub-block table (0 = none)   */
     int32_t reserved;
     int64_t micro_table_bytes;
+    int32_t is_max;       /* 1: range maximum (RMQ_BUILD_MAX)           */
+    int32_t is_int32;     /* 1: int32 elements (RMQ_BUILD_INT32)        */
 } rmq_info_t;
 
 /* rmq_build_ex flags */
 #define RMQ_BUILD_NO_MICRO 1u  /* no sub-block level: same-block queries are
                                   answered by warp-cooperative scans */
+#define RMQ_BUILD_MAX      2u  /* range MAXIMUM (leftmost on ties) instead of
+                                  minimum; NaN still never wins */
+#define RMQ_BUILD_INT32    4u  /* d_vals holds int32 elements (pass the int32
+                                  buffer cast to const float *); the value
+                                  outputs of rmq_query then receive the int32
+                                  bits (pass an int32 buffer cast to float *).
+                                  The role of HRMQ's integer constructors,
+                                  hrmq/includes/RMQRMM64.h:175-178 */
 
 /*
  * Build the index over d_vals[0..n) with block size bs (bs <= 0: default).

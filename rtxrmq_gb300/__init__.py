@@ -72,14 +72,20 @@ class RMQIndex:
     index is used (the index refers to it, it does not copy it).
     """
 
-    def __init__(self, values, bs: int = 0, stream=None, micro: bool = True):
+    def __init__(self, values, bs: int = 0, stream=None, micro: bool = True, op: str = "min"):
+        """values: 1-D float32 or int32 CUDA tensor; op: "min" (the
+        reference's semantics) or "max"; ties resolve to the leftmost index."""
         import torch
-        if values.dtype != torch.float32 or values.dim() != 1:
-            raise TypeError("values must be a 1-D float32 CUDA tensor")
+        if values.dim() != 1 or values.dtype not in (torch.float32, torch.int32):
+            raise TypeError("values must be a 1-D float32 or int32 CUDA tensor")
+        if op not in ("min", "max"):
+            raise ValueError("op must be 'min' or 'max'")
         lib = load()
         self._values = values
+        self._vdtype = values.dtype
         self._h = C.c_void_p()
-        flags = 0 if micro else 1  # RMQ_BUILD_NO_MICRO
+        flags = ((0 if micro else 1) | (2 if op == "max" else 0) |
+                 (4 if values.dtype == torch.int32 else 0))  # RMQ_BUILD_* flags
         check(lib.rmq_build_ex(_dptr(values), values.numel(), int(bs), flags,
                                _stream_handle(stream), C.byref(self._h)))
 
@@ -95,7 +101,7 @@ class RMQIndex:
         q = _check_queries(queries)
         dev = queries.device
         if values and out_val is None:
-            out_val = torch.empty(q, dtype=torch.float32, device=dev)
+            out_val = torch.empty(q, dtype=getattr(self, "_vdtype", torch.float32), device=dev)
         if indices and out_idx is None:
             out_idx = torch.empty(q, dtype=torch.int32, device=dev)
         if not values:
@@ -137,10 +143,11 @@ class RMQIndex:
         """Index for ``values`` read from ``path`` (rmq_load); the values must
         be the ones the index was built from."""
         import torch
-        if values.dtype != torch.float32 or values.dim() != 1:
-            raise TypeError("values must be a 1-D float32 CUDA tensor")
+        if values.dim() != 1 or values.dtype not in (torch.float32, torch.int32):
+            raise TypeError("values must be a 1-D float32 or int32 CUDA tensor")
         self = cls.__new__(cls)
         self._values = values
+        self._vdtype = values.dtype
         self._h = C.c_void_p()
         check(load().rmq_load(_dptr(values), values.numel(), str(path).encode(),
                               _stream_handle(stream), C.byref(self._h)))

@@ -152,7 +152,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
                  rmq_handle_t **out) {
     g_err[0] = '\0';
     if (!out) return set_error(RMQ_EINVAL, "rmq_build: out is NULL");
-    if (flags & ~static_cast<uint32_t>(RMQ_BUILD_NO_MICRO))
+    if (flags & ~static_cast<uint32_t>(RMQ_BUILD_NO_MICRO | RMQ_BUILD_MAX | RMQ_BUILD_INT32))
         return set_error(RMQ_EINVAL, "rmq_build_ex: unknown flags 0x%x", flags);
     *out = nullptr;
     if (n <= 0 || n > 0x7fffffffLL)
@@ -172,6 +172,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     p.A = d_vals;
     p.n = static_cast<uint32_t>(n);
     p.bs = static_cast<uint32_t>(bs);
+    p.kmode = ((flags & RMQ_BUILD_INT32) ? kIntMin : kFloatMin) + ((flags & RMQ_BUILD_MAX) ? 1u : 0u);
     const size_t total = plan_index(p, (flags & RMQ_BUILD_NO_MICRO) != 0);
 
     rmq_handle_t *h = new (std::nothrow) rmq_handle_t;
@@ -412,6 +413,8 @@ int rmq_info(const rmq_handle_t *h, rmq_info_t *info) {
     info->reserved = 0;
     info->micro_table_bytes =
         static_cast<int64_t>(sizeof(Entry) * static_cast<size_t>(h->plan.nmicro) * h->plan.mlevels);
+    info->is_max = (h->plan.kmode & 1u) ? 1 : 0;
+    info->is_int32 = (h->plan.kmode >= kIntMin) ? 1 : 0;
     return RMQ_OK;
 }
 

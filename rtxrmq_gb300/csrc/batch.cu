@@ -83,6 +83,7 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     v.nmicro = 0;
     v.mpre = nullptr;
     v.msuf = nullptr;
+    v.kmode = kFloatMin;
     return v;
 }
 
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(kThreads) batch_kernel(BatchParams P) {
         J.pre = P.ws + a.pre;
         J.suf = P.ws + a.pre + a.n;
         J.bmin = P.ws + a.st;
+        J.kmode = kFloatMin;
         build_unit<ALIGNED>(J, w.y, stage, s_warp);
     }
     grid.sync();
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) batch_kernel(BatchParams P) {
             Entry *cur = P.ws + a.st + static_cast<int64_t>(k) * a.nb;
             const uint32_t half = 1u << (k - 1);
             for (uint32_t j = w.z + threadIdx.x; j < w.z + w.w; j += kThreads)
-                cur[j] = better(prev[j], prev[j + half]);
+                cur[j] = better(prev[j], prev[j + half], kFloatMin);
         }
         grid.sync();
     }
@@ -399,6 +401,7 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
         p.mst = nullptr;
         p.mpre = nullptr;
         p.msuf = nullptr;
+        p.kmode = kFloatMin;
         cudaError_t err = launch_build(p, dev, stream);
         if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run_per_array: build");
         if (qcount[i] == 0) continue;

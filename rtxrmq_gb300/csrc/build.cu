@@ -22,14 +22,14 @@ build_units_kernel(UnitJob J, uint32_t nunits) {
         build_unit<ALIGNED>(J, u, stage, s_warp);
 }
 
-__global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
+__global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k, uint32_t mode) {
     const Entry *prev = st + static_cast<size_t>(k - 1) * nb;
     Entry *cur = st + static_cast<size_t>(k) * nb;
     const uint32_t half = 1u << (k - 1);
     const uint32_t cnt = nb - (1u << k) + 1;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt;
          j += gridDim.x * blockDim.x)
-        cur[j] = better(prev[j], prev[j + half]);
+        cur[j] = better(prev[j], prev[j + half], mode);
 }
 
 // Sub-block level, one warp per 32-element micro-block (lane = element):
@@ -38,14 +38,14 @@ __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
 // its first element) as level 0 of the micro table.
 __global__ void __launch_bounds__(256)
 micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entry *mpre,
-                  Entry *msuf, Entry *mst0) {
+                  Entry *msuf, Entry *mst0, uint32_t mode) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < nmicro; j += warps) {
         const uint32_t g = j * kMicro + lane;
         const bool in = g < n;
-        const uint32_t bits = in ? __float_as_uint(__ldg(A + g)) : 0u;
-        const uint64_t c = in ? ((static_cast<uint64_t>(fkey(bits)) << 32) | g) : ~0ull;
+        const uint32_t bits = in ? ld_u1(A + g) : 0u;
+        const uint64_t c = in ? ((static_cast<uint64_t>(key_of(bits, mode)) << 32) | g) : ~0ull;
         uint64_t p = c, s = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -67,14 +67,14 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
 
 int g_units_per_sm[2] = {0, 0};
 
-cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceInfo &dev,
+cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, uint32_t mode, const DeviceInfo &dev,
                           cudaStream_t s) {
     for (uint32_t k = 1; k < levels; ++k) {
         const uint32_t cnt = nb - (1u << k) + 1;
         uint32_t g = (cnt + 255) / 256;
         const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
         if (g > cap) g = cap;
-        st_level_kernel<<<g, 256, 0, s>>>(st, nb, k);
+        st_level_kernel<<<g, 256, 0, s>>>(st, nb, k, mode);
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return err;
     }
@@ -146,6 +146,7 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     J.pre = p.pre;
     J.suf = p.suf;
     J.bmin = p.st;
+    J.kmode = p.kmode;
     const uint32_t nunits = unit_count(p.nb, J.U);
 
     cudaError_t err;
@@ -166,16 +167,16 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
         build_units_kernel<false><<<grid, kBuildThreads, 0, s>>>(J, nunits);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    err = launch_levels(p.st, p.nb, p.levels, dev, s);
+    err = launch_levels(p.st, p.nb, p.levels, p.kmode, dev, s);
     if (err != cudaSuccess || !p.micro) return err;
 
     uint32_t g = (p.nmicro + 7) / 8;  // 8 warps per CTA, one micro-block per warp
     const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
     if (g > cap) g = cap;
-    micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst);
+    micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst, p.kmode);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    return launch_levels(p.mst, p.nmicro, p.mlevels, dev, s);
+    return launch_levels(p.mst, p.nmicro, p.mlevels, p.kmode, dev, s);
 }
 
 }  // namespace rmq

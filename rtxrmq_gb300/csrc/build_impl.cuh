@@ -11,14 +11,14 @@
 //
 // One CTA owns a "unit": one block when blocks are large, or G whole blocks
 // (G * bs <= 4096 elements) when they are small. A unit is streamed in
-// 4096-element tiles (16 consecutive floats per thread, float4 loads aligned
+// 4096-element tiles (16 consecutive elements per thread, 16-byte loads aligned
 // on absolute element indices): suffix pass right-to-left, then prefix pass
 // left-to-right (re-reading lines the suffix pass just brought into L2), each
 // tile a thread-local scan plus a CTA-wide scan, carried across tiles.
 // Results are staged in shared memory and written with coalesced stores.
 //
 // Segmented scans without flags: every element becomes one 64-bit composite
-//   [segment rank | fkey(value) | local index | -0.0 bit]
+//   [segment rank | key(value) | local index | -0.0 bit]
 // whose unsigned minimum is the leftmost minimum. In the prefix direction
 // earlier blocks of the unit get a larger rank, in the suffix direction later
 // blocks do, so one min-scan over the unit restarts at every block boundary.
@@ -74,22 +74,24 @@ struct UnitJob {
     Entry *pre;   // [n], array-relative
     Entry *suf;   // [n]
     Entry *bmin;  // [nb]
+    uint32_t kmode;  // KeyMode (common.cuh)
 };
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return b < a ? b : a; }
 
 __device__ __forceinline__ uint64_t unit_comp(uint32_t bits, uint32_t local, uint32_t segf,
-                                              const UnitLayout &U) {
+                                              const UnitLayout &U, uint32_t mode) {
     const uint64_t nz = (bits == 0x80000000u) ? 1ull : 0ull;
     return (static_cast<uint64_t>(segf) << U.seg_shift) |
-           (static_cast<uint64_t>(fkey(bits)) << U.key_shift) |
+           (static_cast<uint64_t>(key_of(bits, mode)) << U.key_shift) |
            (static_cast<uint64_t>(local) << 1) | nz;
 }
 
-__device__ __forceinline__ Entry unit_decode(uint64_t c, uint32_t ustart, const UnitLayout &U) {
+__device__ __forceinline__ Entry unit_decode(uint64_t c, uint32_t ustart, const UnitLayout &U,
+                                             uint32_t mode) {
     Entry e;
     const uint32_t key = static_cast<uint32_t>(c >> U.key_shift);
-    e.bits = funkey(key, static_cast<uint32_t>(c & 1ull));
+    e.bits = unkey(key, static_cast<uint32_t>(c & 1ull), mode);
     e.idx = ustart + (static_cast<uint32_t>(c >> 1) & U.local_mask);
     return e;
 }
@@ -152,20 +154,19 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
 
             uint32_t bits[kBuildEPT];
             if (ALIGNED && base + kBuildEPT <= J.limit) {
-                const float4 *src = reinterpret_cast<const float4 *>(J.A + base);
 #pragma unroll
                 for (int v = 0; v < kBuildEPT / 4; ++v) {
-                    const float4 f = __ldg(src + v);
-                    bits[4 * v + 0] = __float_as_uint(f.x);
-                    bits[4 * v + 1] = __float_as_uint(f.y);
-                    bits[4 * v + 2] = __float_as_uint(f.z);
-                    bits[4 * v + 3] = __float_as_uint(f.w);
+                    const uint4 f = ld_u4(J.A + base + 4 * v);
+                    bits[4 * v + 0] = f.x;
+                    bits[4 * v + 1] = f.y;
+                    bits[4 * v + 2] = f.z;
+                    bits[4 * v + 3] = f.w;
                 }
             } else {
 #pragma unroll
                 for (int j = 0; j < kBuildEPT; ++j) {
                     const int64_t g = base + j;
-                    bits[j] = (g >= a_lo && g < a_hi) ? __float_as_uint(__ldg(J.A + g)) : 0u;
+                    bits[j] = (g >= a_lo && g < a_hi) ? ld_u1(J.A + g) : 0u;
                 }
             }
 
@@ -180,7 +181,7 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
                         const uint32_t seg = div31(local, J.dv);
                         segf = suffix ? seg : (U.G - 1 - seg);
                     }
-                    c[j] = unit_comp(bits[j], local, segf, U);
+                    c[j] = unit_comp(bits[j], local, segf, U, J.kmode);
                 } else {
                     c[j] = ~0ull;
                 }
@@ -203,7 +204,8 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
 
 #pragma unroll
             for (int j = 0; j < kBuildEPT; ++j)
-                stage[threadIdx.x * (kBuildEPT + 1) + j] = unit_decode(umin64(c[j], ex), ustart, U);
+                stage[threadIdx.x * (kBuildEPT + 1) + j] =
+                    unit_decode(umin64(c[j], ex), ustart, U, J.kmode);
             __syncthreads();
 
             Entry *out = suffix ? J.suf : J.pre;

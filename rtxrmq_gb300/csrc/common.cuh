@@ -38,21 +38,67 @@ RMQ_HD uint32_t funkey(uint32_t k, uint32_t negzero) {
     return (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
 }
 
-RMQ_HD uint64_t entry_comp(Entry e) {
-    return (static_cast<uint64_t>(fkey(e.bits)) << 32) | e.idx;
+// Key modes: what "best" means for an index. Every mode maps the 32-bit
+// element to an unsigned key whose minimum is the best element, so one
+// unsigned min over (key << 32 | index) returns the leftmost best.
+enum KeyMode : uint32_t {
+    kFloatMin = 0,  // float32, range minimum (the reference's semantics)
+    kFloatMax = 1,  // float32, range maximum
+    kIntMin = 2,    // int32, range minimum
+    kIntMax = 3,    // int32, range maximum
+};
+
+RMQ_HD uint32_t key_of(uint32_t b, uint32_t mode) {
+    switch (mode) {
+    case kFloatMax: {
+        const uint32_t k = fkey(b);
+        return k == 0xffffffffu ? k : ~k;  // NaN stays last
+    }
+    case kIntMin: return b ^ 0x80000000u;
+    case kIntMax: return b ^ 0x7fffffffu;
+    default: return fkey(b);
+    }
 }
 
-// Leftmost minimum of two entries.
-RMQ_HD Entry better(Entry a, Entry b) {
-    return entry_comp(b) < entry_comp(a) ? b : a;
+// Inverse of key_of; `negzero` restores -0.0 in the float modes.
+RMQ_HD uint32_t unkey(uint32_t k, uint32_t negzero, uint32_t mode) {
+    switch (mode) {
+    case kFloatMax: return k == 0xffffffffu ? 0x7fc00000u : funkey(~k, negzero);
+    case kIntMin: return k ^ 0x80000000u;
+    case kIntMax: return k ^ 0x7fffffffu;
+    default: return funkey(k, negzero);
+    }
 }
 
-RMQ_HD Entry entry_max() {
+RMQ_HD uint64_t entry_comp(Entry e, uint32_t mode = kFloatMin) {
+    return (static_cast<uint64_t>(key_of(e.bits, mode)) << 32) | e.idx;
+}
+
+// Leftmost best of two entries.
+RMQ_HD Entry better(Entry a, Entry b, uint32_t mode = kFloatMin) {
+    return entry_comp(b, mode) < entry_comp(a, mode) ? b : a;
+}
+
+// An entry that loses against every real entry in `mode`.
+RMQ_HD Entry entry_max(uint32_t mode = kFloatMin) {
     Entry e;
-    e.bits = 0x7fc00000u;
+    e.bits = unkey(0xffffffffu, 0u, mode);
     e.idx = 0xffffffffu;
     return e;
 }
+
+// Element loads as raw 32-bit words. Elements are never moved through float
+// registers: bit operations on a value that came from one (say an XOR of the
+// sign bit) may be lowered to float instructions that do not keep NaN
+// payloads, and the int32 key modes treat every bit pattern as a value.
+#ifdef __CUDACC__
+__device__ __forceinline__ uint4 ld_u4(const float *p) {
+    return __ldg(reinterpret_cast<const uint4 *>(p));
+}
+__device__ __forceinline__ uint32_t ld_u1(const float *p) {
+    return __ldg(reinterpret_cast<const unsigned int *>(p));
+}
+#endif
 
 // Exact unsigned division of x < 2^31 by a runtime divisor d >= 1:
 //   q = floor(x * m / 2^(31 + s)),  s = ceil(log2 d),  m = ceil(2^(31+s) / d).

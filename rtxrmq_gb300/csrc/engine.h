@@ -43,6 +43,7 @@ struct BuildPlan {
     Entry *mst;        // [mlevels * nmicro]
     Entry *mpre;       // [n] leftmost minimum of A[microstart(i) .. i]
     Entry *msuf;       // [n] leftmost minimum of A[i .. microend(i)]
+    uint32_t kmode;    // KeyMode: float32 / int32 elements, minimum / maximum
 };
 constexpr uint32_t kMicro = 32;
 // levels of the micro table for block size bs (0 when not applicable)

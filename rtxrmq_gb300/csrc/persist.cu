@@ -25,7 +25,7 @@ constexpr size_t kIoChunk = size_t(64) << 20;
 struct FileHeader {
     char magic[16];
     uint32_t version;
-    uint32_t flags;          // RMQ_BUILD_NO_MICRO when built without the sub-block level
+    uint32_t flags;          // rmq_build_ex flags the index was built with
     uint64_t n, bs, nb, levels, nmicro, mlevels;
     uint64_t bytes;          // size of the device allocation that follows
     uint64_t values_print;   // fingerprint of A[0..n)
@@ -45,7 +45,7 @@ __global__ void fingerprint_kernel(const float *__restrict__ A, uint32_t n,
                                    unsigned long long *out) {
     uint64_t acc = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        acc ^= mix64((static_cast<uint64_t>(i) << 32) | __float_as_uint(__ldg(A + i)));
+        acc ^= mix64((static_cast<uint64_t>(i) << 32) | ld_u1(A + i));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) atomicXor(out, static_cast<unsigned long long>(acc));
@@ -100,7 +100,8 @@ int rmq_save(const rmq_handle_t *h, const char *path, rmq_stream_t stream) {
     std::memset(&hd, 0, sizeof(hd));
     std::memcpy(hd.magic, kMagic, sizeof(kMagic));
     hd.version = kVersion;
-    hd.flags = p.micro ? 0u : RMQ_BUILD_NO_MICRO;
+    hd.flags = (p.micro ? 0u : RMQ_BUILD_NO_MICRO) | ((p.kmode & 1u) ? RMQ_BUILD_MAX : 0u) |
+               (p.kmode >= kIntMin ? RMQ_BUILD_INT32 : 0u);
     hd.n = p.n;
     hd.bs = p.bs;
     hd.nb = p.nb;
@@ -162,6 +163,7 @@ int rmq_load(const float *d_vals, int64_t n, const char *path, rmq_stream_t stre
     p.A = d_vals;
     p.n = static_cast<uint32_t>(n);
     p.bs = static_cast<uint32_t>(hd.bs);
+    p.kmode = ((hd.flags & RMQ_BUILD_INT32) ? kIntMin : kFloatMin) + ((hd.flags & RMQ_BUILD_MAX) ? 1u : 0u);
     const size_t bytes = (hd.bs >= 1 && hd.bs <= hd.n)
                              ? plan_index(p, (hd.flags & RMQ_BUILD_NO_MICRO) != 0) : 0;
     if (!bytes || bytes != hd.bytes || p.nb != hd.nb || p.levels != hd.levels ||

@@ -107,6 +107,7 @@ V1View view_of(const BuildPlan &p) {
     v.nmicro = p.micro ? p.nmicro : 0u;
     v.mpre = p.micro ? p.mpre : nullptr;
     v.msuf = p.micro ? p.msuf : nullptr;
+    v.kmode = p.kmode;
     return v;
 }
 

@@ -46,9 +46,10 @@ struct V1View {
     uint32_t nmicro;
     const Entry *mpre;  // in-micro-block prefix / suffix minima
     const Entry *msuf;
+    uint32_t kmode;     // KeyMode: element type and minimum / maximum
 };
 
-// Leftmost minimum of local A[a..b] (b - a < 32, at most 9 float4 loads)
+// Leftmost minimum of local A[a..b] (b - a < 32, at most 9 16-byte loads)
 // computed by one thread.
 template <bool ALIGNED>
 __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, uint32_t b) {
@@ -63,21 +64,21 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
             if (p <= ab) {
                 uint32_t w[4];
                 if (p + 3 < v.limit) {
-                    const float4 f = __ldg(reinterpret_cast<const float4 *>(v.A + p));
-                    w[0] = __float_as_uint(f.x);
-                    w[1] = __float_as_uint(f.y);
-                    w[2] = __float_as_uint(f.z);
-                    w[3] = __float_as_uint(f.w);
+                    const uint4 f = ld_u4(v.A + p);
+                    w[0] = f.x;
+                    w[1] = f.y;
+                    w[2] = f.z;
+                    w[3] = f.w;
                 } else {
 #pragma unroll
                     for (int c = 0; c < 4; ++c)
-                        w[c] = (p + c <= ab) ? __float_as_uint(__ldg(v.A + p + c)) : 0u;
+                        w[c] = (p + c <= ab) ? ld_u1(v.A + p + c) : 0u;
                 }
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     const int64_t g = p + c;
                     if (g >= aa && g <= ab) {
-                        const uint64_t key = (static_cast<uint64_t>(fkey(w[c])) << 32) |
+                        const uint64_t key = (static_cast<uint64_t>(key_of(w[c], v.kmode)) << 32) |
                                              static_cast<uint32_t>(g - v.off);
                         if (key < best) {
                             best = key;
@@ -89,8 +90,8 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
         }
     } else {
         for (int64_t g = aa; g <= ab; ++g) {
-            const uint32_t w = __float_as_uint(__ldg(v.A + g));
-            const uint64_t key = (static_cast<uint64_t>(fkey(w)) << 32) |
+            const uint32_t w = ld_u1(v.A + g);
+            const uint64_t key = (static_cast<uint64_t>(key_of(w, v.kmode)) << 32) |
                                  static_cast<uint32_t>(g - v.off);
             if (key < best) {
                 best = key;
@@ -112,12 +113,12 @@ template <bool ALIGNED>
 __device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
     const uint32_t ml = l >> 5, mr = r >> 5;
     if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
-    Entry e = better(v.msuf[l], v.mpre[r]);
+    Entry e = better(v.msuf[l], v.mpre[r], v.kmode);
     if (mr - ml >= 2u) {
         const uint32_t lo = ml + 1u, hi = mr - 1u;
         const int k = ilog2(hi - lo + 1u);
         const Entry *lvl = v.mst + static_cast<size_t>(k) * v.nmicro;
-        e = better(e, better(lvl[lo], lvl[hi + 1u - (1u << k)]));
+        e = better(e, better(lvl[lo], lvl[hi + 1u - (1u << k)], v.kmode), v.kmode);
     }
     return e;
 }
@@ -130,19 +131,19 @@ struct QueryOut {
 };
 
 __device__ __forceinline__ void put_result(const QueryOut &o, int64_t i, Entry e) {
-    if (o.val) __stcs(o.val + i, __uint_as_float(e.bits));
+    if (o.val) __stcs(reinterpret_cast<unsigned int *>(o.val) + i, e.bits);
     if (o.idx) __stcs(o.idx + i, static_cast<int32_t>(e.idx));
 }
 
 __device__ __forceinline__ void put_invalid(const QueryOut &o, int64_t i) {
-    if (o.val) __stcs(o.val + i, __uint_as_float(0x7fc00000u));
+    if (o.val) __stcs(reinterpret_cast<unsigned int *>(o.val) + i, 0x7fc00000u);
     if (o.idx) __stcs(o.idx + i, -1);
     if (o.invalid) atomicAdd(o.invalid, 1ull);
 }
 
 // Leftmost minimum of local A[l..r] computed by the whole warp. All 32 lanes
 // call it with the same (l, r); every lane gets the result. ALIGNED: the
-// buffer base is 16-byte aligned, so float4 loads on absolute indices are.
+// buffer base is 16-byte aligned, so 16-byte loads on absolute indices are.
 template <bool ALIGNED>
 __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, uint32_t r,
                                                  int lane) {
@@ -152,21 +153,21 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
         for (int64_t p = (al & ~int64_t(3)) + 4 * lane; p <= ar; p += 128) {
             uint32_t b[4];
             if (p + 3 < v.limit) {
-                const float4 f = __ldg(reinterpret_cast<const float4 *>(v.A + p));
-                b[0] = __float_as_uint(f.x);
-                b[1] = __float_as_uint(f.y);
-                b[2] = __float_as_uint(f.z);
-                b[3] = __float_as_uint(f.w);
+                const uint4 f = ld_u4(v.A + p);
+                b[0] = f.x;
+                b[1] = f.y;
+                b[2] = f.z;
+                b[3] = f.w;
             } else {
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    b[c] = (p + c <= ar) ? __float_as_uint(__ldg(v.A + p + c)) : 0u;
+                    b[c] = (p + c <= ar) ? ld_u1(v.A + p + c) : 0u;
             }
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const int64_t g = p + c;
                 if (g >= al && g <= ar) {
-                    const uint64_t k = (static_cast<uint64_t>(fkey(b[c])) << 32) |
+                    const uint64_t k = (static_cast<uint64_t>(key_of(b[c], v.kmode)) << 32) |
                                        static_cast<uint32_t>(g - v.off);
                     best = k < best ? k : best;
                 }
@@ -174,7 +175,7 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
         }
     } else {
         for (int64_t g = al + lane; g <= ar; g += 32) {
-            const uint64_t k = (static_cast<uint64_t>(fkey(__float_as_uint(__ldg(v.A + g)))) << 32) |
+            const uint64_t k = (static_cast<uint64_t>(key_of(ld_u1(v.A + g), v.kmode)) << 32) |
                                static_cast<uint32_t>(g - v.off);
             best = k < best ? k : best;
         }
@@ -184,7 +185,7 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
     const uint32_t cand = (key == kmin) ? static_cast<uint32_t>(best) : 0xffffffffu;
     Entry e;
     e.idx = __reduce_min_sync(0xffffffffu, cand);
-    e.bits = __float_as_uint(__ldg(v.A + v.off + e.idx));
+    e.bits = ld_u1(v.A + v.off + e.idx);
     return e;
 }
 
@@ -238,10 +239,10 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
             const bool use_suf = cross || (same && r[k] == bend);
             const bool use_pre = cross || (same && l[k] == bstart);
             scan[k] = same && !use_suf && !use_pre;
-            es[k] = use_suf ? v.suf[l[k]] : entry_max();
-            ep[k] = use_pre ? v.pre[r[k]] : entry_max();
-            ea[k] = entry_max();
-            eb[k] = entry_max();
+            es[k] = use_suf ? v.suf[l[k]] : entry_max(v.kmode);
+            ep[k] = use_pre ? v.pre[r[k]] : entry_max(v.kmode);
+            ea[k] = entry_max(v.kmode);
+            eb[k] = entry_max(v.kmode);
             if (cross && rB - lB >= 2u) {
                 const uint32_t lo = lB + 1u, hi = rB - 1u;
                 const int lev = ilog2(hi - lo + 1u);
@@ -264,7 +265,7 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                     continue;
                 }
                 const Entry e = scan[k] ? micro_query<ALIGNED>(v, l[k], r[k])
-                                        : better(better(es[k], ep[k]), better(ea[k], eb[k]));
+                                        : better(better(es[k], ep[k], v.kmode), better(ea[k], eb[k], v.kmode), v.kmode);
                 put_result(o, i, e);
             }
             return;
@@ -274,7 +275,7 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
             if (act[k] && !scan[k]) {
                 const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
                 if (ok[k])
-                    put_result(o, i, better(better(es[k], ep[k]), better(ea[k], eb[k])));
+                    put_result(o, i, better(better(es[k], ep[k], v.kmode), better(ea[k], eb[k], v.kmode), v.kmode));
                 else
                     put_invalid(o, i);
             }

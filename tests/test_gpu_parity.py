@@ -361,3 +361,46 @@ def test_save_load_index(cuda, native, oracle_lib, tmp_path):
     (tmp_path / "bad.rmq").write_bytes(bytes(bad))
     with pytest.raises(R.RMQError, match="not an index file"):
         R.RMQIndex.load(dA, tmp_path / "bad.rmq")
+
+
+def np_leftmost(A, Q, op):
+    """Brute-force leftmost argmin / argmax (numpy's first occurrence)."""
+    f = np.argmin if op == "min" else np.argmax
+    return np.array([l + f(A[l:r + 1]) for l, r in Q], dtype=np.int32)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "int32"])
+@pytest.mark.parametrize("op", ["min", "max"])
+@pytest.mark.parametrize("micro", [True, False])
+def test_key_modes(cuda, native, dtype, op, micro):
+    """Range maximum and int32 elements (the role of HRMQ's integer
+    constructors): leftmost best, exact values, every block-size class."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(77)
+    n = 5000
+    if dtype == "int32":
+        A = rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32)
+        A[rng.integers(0, n, 500)] = rng.integers(-3, 3, 500)  # ties, around zero
+        A[rng.integers(0, n, 20)] = np.iinfo(np.int32).max
+        A[rng.integers(0, n, 20)] = np.iinfo(np.int32).min
+    else:
+        A = rng.standard_normal(n).astype(np.float32)
+        A[rng.integers(0, n, 300)] = 0.0
+        A[rng.integers(0, n, 300)] = -0.0
+        A[rng.integers(0, n, 20)] = np.inf
+        A[rng.integers(0, n, 20)] = -np.inf
+    Q = np.concatenate([R.gen_queries(1500, n, L, 5 + L) for L in (-1, -3, 1, 2, 31, 33, 100, 700)])
+    ei = np_leftmost(A, Q, op)
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    for bs in (1, 7, 64, 96, 1024, n):
+        with R.RMQIndex(dA, bs, micro=micro, op=op) as ix:
+            inf = ix.info()
+            assert inf["is_max"] == (op == "max") and inf["is_int32"] == (dtype == "int32")
+            v, i = ix.query(dQ)
+            torch.cuda.synchronize()
+            i, v = i.cpu().numpy(), v.cpu().numpy()
+        np.testing.assert_array_equal(i, ei)
+        np.testing.assert_array_equal(v.view(np.uint32), A[ei].view(np.uint32))
