@@ -30,6 +30,11 @@
 
 namespace cg = cooperative_groups;
 
+// CTAs per SM the persistent batch kernel is compiled for (a register bound).
+#ifndef RMQ_BATCH_MINB
+#define RMQ_BATCH_MINB 4
+#endif
+
 namespace rmq {
 namespace {
 
@@ -87,29 +92,33 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     return v;
 }
 
+__device__ __forceinline__ UnitJob unit_job(const BatchParams &P, uint32_t array) {
+    const BatchArray a = P.arrays[array];
+    UnitJob J;
+    J.A = P.A;
+    J.off = a.off;
+    J.limit = P.limit;
+    J.n = a.n;
+    J.bs = a.bs;
+    J.U = a.U;
+    J.dv = a.dv;
+    J.pre = P.ws + a.pre;
+    J.suf = P.ws + a.pre + a.n;
+    J.bmin = P.ws + a.st;
+    J.kmode = kFloatMin;
+    return J;
+}
+
 template <bool ALIGNED>
-__global__ void __launch_bounds__(kThreads) batch_kernel(BatchParams P) {
+__global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchParams P) {
     __shared__ Entry stage[kStageEntries];
-    __shared__ uint64_t s_warp[kBuildWarps];
+    __shared__ uint64_t s_warp[kWarpSlots];
     cg::grid_group grid = cg::this_grid();
 
     // A: units
     for (int32_t it = blockIdx.x; it < P.nbuild; it += gridDim.x) {
         const uint2 w = P.build[it];
-        const BatchArray a = P.arrays[w.x];
-        UnitJob J;
-        J.A = P.A;
-        J.off = a.off;
-        J.limit = P.limit;
-        J.n = a.n;
-        J.bs = a.bs;
-        J.U = a.U;
-        J.dv = a.dv;
-        J.pre = P.ws + a.pre;
-        J.suf = P.ws + a.pre + a.n;
-        J.bmin = P.ws + a.st;
-        J.kmode = kFloatMin;
-        build_unit<ALIGNED>(J, w.y, stage, s_warp);
+        build_unit<ALIGNED, kFloatMin>(unit_job(P, w.x), w.y, stage, s_warp);
     }
     grid.sync();
 
@@ -157,6 +166,7 @@ scatter_grad_kernel(const BatchArray *arrays, const uint4 *qitems, int32_t nqite
 }
 
 int g_batch_per_sm[2] = {0, 0};
+
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 

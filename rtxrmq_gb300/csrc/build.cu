@@ -10,16 +10,31 @@
 #include "build_impl.cuh"
 #include "engine.h"
 
+// CTAs per SM the unit kernel is compiled for (a register bound).
+#ifndef RMQ_BUILD_MINB
+#define RMQ_BUILD_MINB 4
+#endif
+
 namespace rmq {
 namespace {
 
-template <bool ALIGNED>
-__global__ void __launch_bounds__(kBuildThreads)
+template <bool ALIGNED, uint32_t MODE>
+__global__ void __launch_bounds__(kBuildThreads, RMQ_BUILD_MINB)
 build_units_kernel(UnitJob J, uint32_t nunits) {
     __shared__ Entry stage[kStageEntries];
-    __shared__ uint64_t s_warp[kBuildWarps];
+    __shared__ uint64_t s_warp[kWarpSlots];
     for (uint32_t u = blockIdx.x; u < nunits; u += gridDim.x)
-        build_unit<ALIGNED>(J, u, stage, s_warp);
+        build_unit<ALIGNED, MODE>(J, u, stage, s_warp);
+}
+
+template <bool ALIGNED>
+void launch_units(const UnitJob &J, uint32_t nunits, uint32_t grid, cudaStream_t s) {
+    switch (J.kmode) {
+    case kFloatMax: build_units_kernel<ALIGNED, kFloatMax><<<grid, kBuildThreads, 0, s>>>(J, nunits); break;
+    case kIntMin: build_units_kernel<ALIGNED, kIntMin><<<grid, kBuildThreads, 0, s>>>(J, nunits); break;
+    case kIntMax: build_units_kernel<ALIGNED, kIntMax><<<grid, kBuildThreads, 0, s>>>(J, nunits); break;
+    default: build_units_kernel<ALIGNED, kFloatMin><<<grid, kBuildThreads, 0, s>>>(J, nunits); break;
+    }
 }
 
 __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k, uint32_t mode) {
@@ -152,19 +167,21 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     cudaError_t err;
     int &per_sm = g_units_per_sm[p.aligned ? 1 : 0];
     if (per_sm == 0) {
+        // every key mode compiles to the same resources; the float-min
+        // instantiation stands for all four
         err = p.aligned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, build_units_kernel<true>, kBuildThreads, 0)
+                              &per_sm, build_units_kernel<true, kFloatMin>, kBuildThreads, 0)
                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, build_units_kernel<false>, kBuildThreads, 0);
+                              &per_sm, build_units_kernel<false, kFloatMin>, kBuildThreads, 0);
         if (err != cudaSuccess) return err;
         if (per_sm < 1) per_sm = 1;
     }
     uint32_t grid = static_cast<uint32_t>(dev.sms) * static_cast<uint32_t>(per_sm);
     if (grid > nunits) grid = nunits;
     if (p.aligned)
-        build_units_kernel<true><<<grid, kBuildThreads, 0, s>>>(J, nunits);
+        launch_units<true>(J, nunits, grid, s);
     else
-        build_units_kernel<false><<<grid, kBuildThreads, 0, s>>>(J, nunits);
+        launch_units<false>(J, nunits, grid, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     err = launch_levels(p.st, p.nb, p.levels, p.kmode, dev, s);

@@ -34,6 +34,7 @@ constexpr int kBuildTile = kBuildThreads * kBuildEPT;   // 4096
 constexpr int kBuildWarps = kBuildThreads / 32;
 constexpr uint32_t kUnitTarget = 4096;                  // elements per multi-block unit
 constexpr int kStageEntries = kBuildTile + kBuildTile / 16;
+constexpr int kWarpSlots = 2 * kBuildWarps;             // shared words for the CTA scans
 
 struct UnitLayout {
     uint32_t G;           // blocks per unit
@@ -78,6 +79,17 @@ struct UnitJob {
 };
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return b < a ? b : a; }
+
+// Whether unit u lies inside one tile, and the tile's first element t0
+// (absolute; a 16-byte boundary when ALIGNED).
+template <bool ALIGNED>
+__device__ __forceinline__ bool unit_tile(const UnitJob &J, uint32_t u, int64_t &t0) {
+    const uint32_t ustart = u * J.U.G * J.bs;
+    const uint32_t ulen = min(ustart + J.U.G * J.bs, J.n) - ustart;
+    const int64_t a_lo = J.off + ustart;
+    t0 = ALIGNED ? (a_lo & ~int64_t(3)) : a_lo;
+    return static_cast<uint32_t>(a_lo - t0) + ulen <= static_cast<uint32_t>(kBuildTile);
+}
 
 __device__ __forceinline__ uint64_t unit_comp(uint32_t bits, uint32_t local, uint32_t segf,
                                               const UnitLayout &U, uint32_t mode) {
@@ -129,11 +141,12 @@ __device__ __forceinline__ uint64_t cta_exclusive_min(uint64_t v, uint64_t *s_wa
     return umin64(ex, wex);
 }
 
-// Build unit `u` of job J with the whole CTA (kBuildThreads threads).
-// stage: kStageEntries entries of shared memory; s_warp: kBuildWarps words.
-template <bool ALIGNED>
-__device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *stage,
-                                           uint64_t *s_warp) {
+// Build unit `u` of job J with the whole CTA (kBuildThreads threads), in
+// as many tiles as it spans: suffix pass, then prefix pass.
+// stage: kStageEntries entries of shared memory; s_warp: kWarpSlots words.
+template <bool ALIGNED, uint32_t MODE>
+__device__ __forceinline__ void build_unit_tiles(const UnitJob &J, uint32_t u, Entry *stage,
+                                                 uint64_t *s_warp) {
     const UnitLayout U = J.U;
     const uint32_t ustart = u * U.G * J.bs;
     const uint32_t uend = min(ustart + U.G * J.bs, J.n);
@@ -181,7 +194,7 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
                         const uint32_t seg = div31(local, J.dv);
                         segf = suffix ? seg : (U.G - 1 - seg);
                     }
-                    c[j] = unit_comp(bits[j], local, segf, U, J.kmode);
+                    c[j] = unit_comp(bits[j], local, segf, U, MODE);
                 } else {
                     c[j] = ~0ull;
                 }
@@ -205,7 +218,7 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
 #pragma unroll
             for (int j = 0; j < kBuildEPT; ++j)
                 stage[threadIdx.x * (kBuildEPT + 1) + j] =
-                    unit_decode(umin64(c[j], ex), ustart, U, J.kmode);
+                    unit_decode(umin64(c[j], ex), ustart, U, MODE);
             __syncthreads();
 
             Entry *out = suffix ? J.suf : J.pre;
@@ -232,6 +245,181 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
             }
             __syncthreads();
         }
+    }
+}
+
+// Exclusive min-scans of two values per thread across the CTA: `vp` in
+// thread order, `vs` in reverse thread order, one barrier for both.
+__device__ __forceinline__ void cta_exclusive_min2(uint64_t vp, uint64_t vs, uint64_t *s_warp,
+                                                   uint64_t &xp, uint64_t &xs) {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    uint64_t ip = vp, is = vs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t tp = __shfl_up_sync(0xffffffffu, ip, o);
+        const uint64_t ts = __shfl_down_sync(0xffffffffu, is, o);
+        if (lane >= o) ip = umin64(ip, tp);
+        if (lane + o < 32) is = umin64(is, ts);
+    }
+    uint64_t ep = __shfl_up_sync(0xffffffffu, ip, 1);
+    uint64_t es = __shfl_down_sync(0xffffffffu, is, 1);
+    if (lane == 0) ep = ~0ull;
+    if (lane == 31) es = ~0ull;
+    if (lane == 31) s_warp[warp] = ip;
+    if (lane == 0) s_warp[kBuildWarps + warp] = is;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < kBuildWarps; ++w) {
+        if (w < warp) ep = umin64(ep, s_warp[w]);
+        if (w > warp) es = umin64(es, s_warp[kBuildWarps + w]);
+    }
+    xp = ep;
+    xs = es;
+}
+
+// Build a unit that lies inside one tile (every unit of bs <= 4096 whose
+// first element is at most (tile - unit length) past a 16-byte boundary):
+// the values are loaded once and both scans run on them, with one CTA scan
+// for the two directions. Positions are 32-bit offsets in the unit; the
+// composite is [segment rank (MULTI) | key | unit offset | -0.0 bit] with
+// constant shifts; block minima are read from the staged prefix results at
+// each block's last element.
+template <bool ALIGNED, uint32_t MODE, bool MULTI>
+__device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, Entry *stage,
+                                                uint64_t *s_warp) {
+    const uint32_t G = MULTI ? J.U.G : 1u;
+    const uint32_t ustart = u * G * J.bs;
+    const uint32_t ulen = min(ustart + G * J.bs, J.n) - ustart;
+    const int64_t a_lo = J.off + ustart;
+    const int64_t t0 = ALIGNED ? (a_lo & ~int64_t(3)) : a_lo;
+    const int32_t lead = static_cast<int32_t>(a_lo - t0);
+    const int64_t base = t0 + static_cast<int64_t>(threadIdx.x) * kBuildEPT;
+    const int32_t ul0 = static_cast<int32_t>(threadIdx.x) * kBuildEPT - lead;
+
+    uint32_t bits[kBuildEPT];
+    if (ALIGNED && base + kBuildEPT <= J.limit) {
+#pragma unroll
+        for (int v = 0; v < kBuildEPT / 4; ++v) {
+            const uint4 f = ld_u4(J.A + base + 4 * v);
+            bits[4 * v + 0] = f.x;
+            bits[4 * v + 1] = f.y;
+            bits[4 * v + 2] = f.z;
+            bits[4 * v + 3] = f.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kBuildEPT; ++j)
+            bits[j] = (static_cast<uint32_t>(ul0 + j) < ulen) ? ld_u1(J.A + base + j) : 0u;
+    }
+
+    constexpr bool kFloat = (MODE == kFloatMin || MODE == kFloatMax);
+    uint64_t cb[kBuildEPT];
+    uint64_t agg_p = ~0ull, agg_s = ~0ull;
+#pragma unroll
+    for (int j = 0; j < kBuildEPT; ++j) {
+        const uint32_t ul = static_cast<uint32_t>(ul0 + j);
+        const bool valid = ul < ulen;
+        const uint32_t nz = (kFloat && bits[j] == 0x80000000u) ? 1u : 0u;
+        const uint32_t key = key_of(bits[j], MODE);
+        const uint64_t c = MULTI ? ((static_cast<uint64_t>(key) << 17) | (ul << 1) | nz)
+                                 : ((static_cast<uint64_t>(key) << 32) | (ul << 1) | nz);
+        cb[j] = valid ? c : ~0ull;
+        if (MULTI) {
+            const uint32_t seg = div31(valid ? ul : 0u, J.dv);
+            agg_p = umin64(agg_p, cb[j] | (static_cast<uint64_t>(G - 1u - seg) << 49));
+            agg_s = umin64(agg_s, cb[j] | (static_cast<uint64_t>(seg) << 49));
+        } else {
+            agg_p = umin64(agg_p, cb[j]);
+        }
+    }
+    if (!MULTI) agg_s = agg_p;
+    uint64_t ex_p, ex_s;
+    cta_exclusive_min2(agg_p, agg_s, s_warp, ex_p, ex_s);
+
+    auto decode = [&](uint64_t c) {
+        Entry e;
+        const uint32_t key = MULTI ? static_cast<uint32_t>(c >> 17) : static_cast<uint32_t>(c >> 32);
+        const uint32_t lo = static_cast<uint32_t>(c);
+        e.bits = unkey(key, lo & 1u, MODE);
+        e.idx = ustart + (MULTI ? ((lo >> 1) & 0xffffu) : (lo >> 1));
+        return e;
+    };
+
+    // prefix minima
+    uint64_t run = ex_p;
+#pragma unroll
+    for (int j = 0; j < kBuildEPT; ++j) {
+        uint64_t c = cb[j];
+        if (MULTI) {
+            const uint32_t ul = static_cast<uint32_t>(ul0 + j);
+            const uint32_t seg = div31(ul < ulen ? ul : 0u, J.dv);
+            c |= static_cast<uint64_t>(G - 1u - seg) << 49;
+        }
+        run = umin64(run, c);
+        stage[threadIdx.x * (kBuildEPT + 1) + j] = decode(run);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < kBuildEPT; ++k) {
+        const uint32_t e = threadIdx.x + k * kBuildThreads;
+        const uint32_t ul = e - static_cast<uint32_t>(lead);
+        if (ul < ulen) {
+            const Entry en = stage[e + (e >> 4)];
+            __stcs(reinterpret_cast<uint2 *>(J.pre + ustart + ul), make_uint2(en.bits, en.idx));
+        }
+    }
+    {
+        // block minimum = prefix minimum at the block's last element
+        const uint32_t nblk = MULTI ? div31(ulen - 1u, J.dv) + 1u : 1u;
+        for (uint32_t b = threadIdx.x; b < nblk; b += kBuildThreads) {
+            const uint32_t last = min((b + 1u) * J.bs, ulen) - 1u;
+            const uint32_t e = last + static_cast<uint32_t>(lead);
+            J.bmin[u * G + b] = stage[e + (e >> 4)];
+        }
+    }
+    __syncthreads();
+
+    // suffix minima
+    run = ex_s;
+#pragma unroll
+    for (int j = kBuildEPT - 1; j >= 0; --j) {
+        uint64_t c = cb[j];
+        if (MULTI) {
+            const uint32_t ul = static_cast<uint32_t>(ul0 + j);
+            const uint32_t seg = div31(ul < ulen ? ul : 0u, J.dv);
+            c |= static_cast<uint64_t>(seg) << 49;
+        }
+        run = umin64(run, c);
+        stage[threadIdx.x * (kBuildEPT + 1) + j] = decode(run);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < kBuildEPT; ++k) {
+        const uint32_t e = threadIdx.x + k * kBuildThreads;
+        const uint32_t ul = e - static_cast<uint32_t>(lead);
+        if (ul < ulen) {
+            const Entry en = stage[e + (e >> 4)];
+            __stcs(reinterpret_cast<uint2 *>(J.suf + ustart + ul), make_uint2(en.bits, en.idx));
+        }
+    }
+    // The next unit's first shared-memory writes (s_warp, stage) come after
+    // a barrier every thread reaches only when it has finished these reads.
+}
+
+// Build unit `u`: one-tile units with the single-pass builder, others with
+// the tile-streaming one. The choice is uniform across the CTA.
+template <bool ALIGNED, uint32_t MODE>
+__device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *stage,
+                                           uint64_t *s_warp) {
+    int64_t t0;
+    if (unit_tile<ALIGNED>(J, u, t0)) {
+        if (J.U.G > 1)
+            build_unit_tile<ALIGNED, MODE, true>(J, u, stage, s_warp);
+        else
+            build_unit_tile<ALIGNED, MODE, false>(J, u, stage, s_warp);
+    } else {
+        build_unit_tiles<ALIGNED, MODE>(J, u, stage, s_warp);
     }
 }
 
