@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
             Entry *cur = P.ws + a.st + static_cast<int64_t>(k) * a.nb;
             const uint32_t half = 1u << (k - 1);
             for (uint32_t j = w.z + threadIdx.x; j < w.z + w.w; j += kThreads)
-                cur[j] = better(prev[j], prev[j + half], kFloatMin);
+                cur[j] = better(prev[j], prev[j + half]);
         }
         grid.sync();
     }

@@ -37,14 +37,14 @@ void launch_units(const UnitJob &J, uint32_t nunits, uint32_t grid, cudaStream_t
     }
 }
 
-__global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k, uint32_t mode) {
+__global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
     const Entry *prev = st + static_cast<size_t>(k - 1) * nb;
     Entry *cur = st + static_cast<size_t>(k) * nb;
     const uint32_t half = 1u << (k - 1);
     const uint32_t cnt = nb - (1u << k) + 1;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt;
          j += gridDim.x * blockDim.x)
-        cur[j] = better(prev[j], prev[j + half], mode);
+        cur[j] = better(prev[j], prev[j + half]);
 }
 
 // Sub-block level, one warp per 32-element micro-block (lane = element):
@@ -59,8 +59,7 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
     for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < nmicro; j += warps) {
         const uint32_t g = j * kMicro + lane;
         const bool in = g < n;
-        const uint32_t bits = in ? ld_u1(A + g) : 0u;
-        const uint64_t c = in ? ((static_cast<uint64_t>(key_of(bits, mode)) << 32) | g) : ~0ull;
+        const uint64_t c = in ? make_entry(ld_u1(A + g), g, mode) : kEntryNone;
         uint64_t p = c, s = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -69,27 +68,24 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
             if (lane >= static_cast<uint32_t>(o) && tp < p) p = tp;
             if (lane + o < 32u && ts < s) s = ts;
         }
-        // raw bits of each argmin come from the lane that holds it
-        const uint32_t pb = __shfl_sync(0xffffffffu, bits, static_cast<uint32_t>(p) & 31u);
-        const uint32_t sb = __shfl_sync(0xffffffffu, bits, static_cast<uint32_t>(s) & 31u);
         if (in) {
-            __stcs(reinterpret_cast<uint2 *>(mpre + g), make_uint2(pb, static_cast<uint32_t>(p)));
-            __stcs(reinterpret_cast<uint2 *>(msuf + g), make_uint2(sb, static_cast<uint32_t>(s)));
-            if (lane == 0) mst0[j] = Entry{sb, static_cast<uint32_t>(s)};
+            st_entry(mpre + g, p);
+            st_entry(msuf + g, s);
+            if (lane == 0) mst0[j] = s;
         }
     }
 }
 
 int g_units_per_sm[2] = {0, 0};
 
-cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, uint32_t mode, const DeviceInfo &dev,
+cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceInfo &dev,
                           cudaStream_t s) {
     for (uint32_t k = 1; k < levels; ++k) {
         const uint32_t cnt = nb - (1u << k) + 1;
         uint32_t g = (cnt + 255) / 256;
         const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
         if (g > cap) g = cap;
-        st_level_kernel<<<g, 256, 0, s>>>(st, nb, k, mode);
+        st_level_kernel<<<g, 256, 0, s>>>(st, nb, k);
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess) return err;
     }
@@ -184,7 +180,7 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
         launch_units<false>(J, nunits, grid, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    err = launch_levels(p.st, p.nb, p.levels, p.kmode, dev, s);
+    err = launch_levels(p.st, p.nb, p.levels, dev, s);
     if (err != cudaSuccess || !p.micro) return err;
 
     uint32_t g = (p.nmicro + 7) / 8;  // 8 warps per CTA, one micro-block per warp
@@ -193,7 +189,7 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst, p.kmode);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    return launch_levels(p.mst, p.nmicro, p.mlevels, p.kmode, dev, s);
+    return launch_levels(p.mst, p.nmicro, p.mlevels, dev, s);
 }
 
 }  // namespace rmq

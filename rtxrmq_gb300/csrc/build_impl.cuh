@@ -93,19 +93,23 @@ __device__ __forceinline__ bool unit_tile(const UnitJob &J, uint32_t u, int64_t 
 
 __device__ __forceinline__ uint64_t unit_comp(uint32_t bits, uint32_t local, uint32_t segf,
                                               const UnitLayout &U, uint32_t mode) {
-    const uint64_t nz = (bits == 0x80000000u) ? 1ull : 0ull;
+    const uint64_t nz = negzero_of(bits, mode);
     return (static_cast<uint64_t>(segf) << U.seg_shift) |
            (static_cast<uint64_t>(key_of(bits, mode)) << U.key_shift) |
            (static_cast<uint64_t>(local) << 1) | nz;
 }
 
-__device__ __forceinline__ Entry unit_decode(uint64_t c, uint32_t ustart, const UnitLayout &U,
-                                             uint32_t mode) {
-    Entry e;
+// Unit composite -> index entry (common.cuh) of the array-relative index.
+__device__ __forceinline__ Entry unit_decode(uint64_t c, uint32_t ustart, const UnitLayout &U) {
     const uint32_t key = static_cast<uint32_t>(c >> U.key_shift);
-    e.bits = unkey(key, static_cast<uint32_t>(c & 1ull), mode);
-    e.idx = ustart + (static_cast<uint32_t>(c >> 1) & U.local_mask);
-    return e;
+    const uint32_t idx = ustart + (static_cast<uint32_t>(c >> 1) & U.local_mask);
+    return (static_cast<uint64_t>(key) << 32) | (idx << 1) | (static_cast<uint32_t>(c) & 1u);
+}
+
+// Streaming store of one entry (written once, read by later kernels).
+__device__ __forceinline__ void st_entry(Entry *p, Entry e) {
+    __stcs(reinterpret_cast<uint2 *>(p),
+           make_uint2(static_cast<uint32_t>(e), static_cast<uint32_t>(e >> 32)));
 }
 
 // Exclusive min-scan of one value per thread across the CTA, in thread order
@@ -218,7 +222,7 @@ __device__ __forceinline__ void build_unit_tiles(const UnitJob &J, uint32_t u, E
 #pragma unroll
             for (int j = 0; j < kBuildEPT; ++j)
                 stage[threadIdx.x * (kBuildEPT + 1) + j] =
-                    unit_decode(umin64(c[j], ex), ustart, U, MODE);
+                    unit_decode(umin64(c[j], ex), ustart, U);
             __syncthreads();
 
             Entry *out = suffix ? J.suf : J.pre;
@@ -229,7 +233,7 @@ __device__ __forceinline__ void build_unit_tiles(const UnitJob &J, uint32_t u, E
                 if (g >= a_lo && g < a_hi) {
                     const Entry en = stage[e + (e >> 4)];
                     const uint32_t local = static_cast<uint32_t>(g - J.off);
-                    __stcs(reinterpret_cast<uint2 *>(out + local), make_uint2(en.bits, en.idx));
+                    st_entry(out + local, en);
                     if (!suffix) {
                         // block minimum = prefix minimum at the block's last element
                         const uint32_t ul = local - ustart;
@@ -337,13 +341,13 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
     uint64_t ex_p, ex_s;
     cta_exclusive_min2(agg_p, agg_s, s_warp, ex_p, ex_s);
 
-    auto decode = [&](uint64_t c) {
-        Entry e;
-        const uint32_t key = MULTI ? static_cast<uint32_t>(c >> 17) : static_cast<uint32_t>(c >> 32);
+    // unit composite -> entry: for one block per unit it only moves the
+    // offset to the array-relative index
+    auto decode = [&](uint64_t c) -> Entry {
+        if (!MULTI) return c + (static_cast<uint64_t>(ustart) << 1);
         const uint32_t lo = static_cast<uint32_t>(c);
-        e.bits = unkey(key, lo & 1u, MODE);
-        e.idx = ustart + (MULTI ? ((lo >> 1) & 0xffffu) : (lo >> 1));
-        return e;
+        const uint32_t idx = ustart + ((lo >> 1) & 0xffffu);
+        return (static_cast<uint64_t>(static_cast<uint32_t>(c >> 17)) << 32) | (idx << 1) | (lo & 1u);
     };
 
     // prefix minima
@@ -365,8 +369,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         const uint32_t e = threadIdx.x + k * kBuildThreads;
         const uint32_t ul = e - static_cast<uint32_t>(lead);
         if (ul < ulen) {
-            const Entry en = stage[e + (e >> 4)];
-            __stcs(reinterpret_cast<uint2 *>(J.pre + ustart + ul), make_uint2(en.bits, en.idx));
+            st_entry(J.pre + ustart + ul, stage[e + (e >> 4)]);
         }
     }
     {
@@ -399,8 +402,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         const uint32_t e = threadIdx.x + k * kBuildThreads;
         const uint32_t ul = e - static_cast<uint32_t>(lead);
         if (ul < ulen) {
-            const Entry en = stage[e + (e >> 4)];
-            __stcs(reinterpret_cast<uint2 *>(J.suf + ustart + ul), make_uint2(en.bits, en.idx));
+            st_entry(J.suf + ustart + ul, stage[e + (e >> 4)]);
         }
     }
     // The next unit's first shared-memory writes (s_warp, stage) come after

@@ -1,13 +1,14 @@
 // common.cuh -- types and helpers shared by the build, query, batch and
 // gradient kernels and by the host code of the C ABI.
 //
-// Ordering. Every comparison in the engine is made on a 64-bit composite
-//     (fkey(value) << 32) | index
+// Ordering. Every element is compared through a 64-bit composite
+//     (key(value) << 32) | (index << 1) | negzero
 // so that a plain unsigned min returns the smallest value and, among equal
-// values, the smallest index. fkey() is order preserving for the float `<`
-// used by the reference's oracles (src/cpu_methods.h:42-53,
+// values, the smallest index. For floats key() = fkey(), order preserving
+// for the float `<` used by the reference's oracles (src/cpu_methods.h:42-53,
 // src/cuda_methods.cuh:23-42): -0.0 and +0.0 map to one key, NaN maps above
-// +inf. Stored entries keep the raw float bits, so results are bit-exact.
+// +inf; `negzero` marks -0.0 so its bits come back exactly. The index tables
+// store these composites, so every comparison is one unsigned min.
 #pragma once
 
 #include <cstdint>
@@ -16,12 +17,6 @@
 #define RMQ_HD __host__ __device__ __forceinline__
 
 namespace rmq {
-
-// One structure entry: raw float bits of a minimum and its global index.
-struct __align__(8) Entry {
-    uint32_t bits;
-    uint32_t idx;
-};
 
 // Order-preserving map float bits -> uint32 (see file comment).
 RMQ_HD uint32_t fkey(uint32_t b) {
@@ -70,22 +65,30 @@ RMQ_HD uint32_t unkey(uint32_t k, uint32_t negzero, uint32_t mode) {
     }
 }
 
-RMQ_HD uint64_t entry_comp(Entry e, uint32_t mode = kFloatMin) {
-    return (static_cast<uint64_t>(key_of(e.bits, mode)) << 32) | e.idx;
+// One structure entry: the composite of its element (file comment). Indices
+// are below 2^31, so `index << 1` fits the low word.
+using Entry = uint64_t;
+
+// An entry that loses against every real entry.
+constexpr Entry kEntryNone = ~0ull;
+
+RMQ_HD uint32_t negzero_of(uint32_t b, uint32_t mode) {
+    return ((mode == kFloatMin || mode == kFloatMax) && b == 0x80000000u) ? 1u : 0u;
+}
+
+RMQ_HD Entry make_entry(uint32_t b, uint32_t idx, uint32_t mode) {
+    return (static_cast<uint64_t>(key_of(b, mode)) << 32) | (idx << 1) | negzero_of(b, mode);
+}
+
+RMQ_HD uint32_t entry_idx(Entry e) { return static_cast<uint32_t>(e) >> 1; }
+
+// The element's bits (a NaN comes back as the canonical quiet NaN).
+RMQ_HD uint32_t entry_bits(Entry e, uint32_t mode) {
+    return unkey(static_cast<uint32_t>(e >> 32), static_cast<uint32_t>(e) & 1u, mode);
 }
 
 // Leftmost best of two entries.
-RMQ_HD Entry better(Entry a, Entry b, uint32_t mode = kFloatMin) {
-    return entry_comp(b, mode) < entry_comp(a, mode) ? b : a;
-}
-
-// An entry that loses against every real entry in `mode`.
-RMQ_HD Entry entry_max(uint32_t mode = kFloatMin) {
-    Entry e;
-    e.bits = unkey(0xffffffffu, 0u, mode);
-    e.idx = 0xffffffffu;
-    return e;
-}
+RMQ_HD Entry better(Entry a, Entry b) { return b < a ? b : a; }
 
 // Element loads as raw 32-bit words. Elements are never moved through float
 // registers: bit operations on a value that came from one (say an XOR of the

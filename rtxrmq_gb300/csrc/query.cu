@@ -63,10 +63,7 @@ scan_kernel(const float *__restrict__ A, uint32_t n, QueryOut o, int64_t q) {
                 mi = j;
             }
         }
-        Entry e;
-        e.bits = __float_as_uint(m);
-        e.idx = mi;
-        put_result(o, i, e);
+        put_bits_idx(o, i, __float_as_uint(m), mi);
     }
 }
 

@@ -54,8 +54,7 @@ struct V1View {
 template <bool ALIGNED>
 __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, uint32_t b) {
     const int64_t aa = v.off + a, ab = v.off + b;
-    uint64_t best = ~0ull;
-    uint32_t best_bits = 0x7fc00000u;
+    Entry best = kEntryNone;
     if (ALIGNED) {
         const int64_t p0 = aa & ~int64_t(3);
 #pragma unroll
@@ -77,32 +76,16 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     const int64_t g = p + c;
-                    if (g >= aa && g <= ab) {
-                        const uint64_t key = (static_cast<uint64_t>(key_of(w[c], v.kmode)) << 32) |
-                                             static_cast<uint32_t>(g - v.off);
-                        if (key < best) {
-                            best = key;
-                            best_bits = w[c];
-                        }
-                    }
+                    if (g >= aa && g <= ab)
+                        best = better(best, make_entry(w[c], static_cast<uint32_t>(g - v.off), v.kmode));
                 }
             }
         }
     } else {
-        for (int64_t g = aa; g <= ab; ++g) {
-            const uint32_t w = ld_u1(v.A + g);
-            const uint64_t key = (static_cast<uint64_t>(key_of(w, v.kmode)) << 32) |
-                                 static_cast<uint32_t>(g - v.off);
-            if (key < best) {
-                best = key;
-                best_bits = w;
-            }
-        }
+        for (int64_t g = aa; g <= ab; ++g)
+            best = better(best, make_entry(ld_u1(v.A + g), static_cast<uint32_t>(g - v.off), v.kmode));
     }
-    Entry e;
-    e.bits = best_bits;
-    e.idx = static_cast<uint32_t>(best);
-    return e;
+    return best;
 }
 
 // Same-block query through the sub-block level: the partial micro-blocks at
@@ -113,12 +96,12 @@ template <bool ALIGNED>
 __device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
     const uint32_t ml = l >> 5, mr = r >> 5;
     if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
-    Entry e = better(v.msuf[l], v.mpre[r], v.kmode);
+    Entry e = better(v.msuf[l], v.mpre[r]);
     if (mr - ml >= 2u) {
         const uint32_t lo = ml + 1u, hi = mr - 1u;
         const int k = ilog2(hi - lo + 1u);
         const Entry *lvl = v.mst + static_cast<size_t>(k) * v.nmicro;
-        e = better(e, better(lvl[lo], lvl[hi + 1u - (1u << k)], v.kmode), v.kmode);
+        e = better(e, better(lvl[lo], lvl[hi + 1u - (1u << k)]));
     }
     return e;
 }
@@ -130,9 +113,14 @@ struct QueryOut {
     unsigned long long *invalid;
 };
 
-__device__ __forceinline__ void put_result(const QueryOut &o, int64_t i, Entry e) {
-    if (o.val) __stcs(reinterpret_cast<unsigned int *>(o.val) + i, e.bits);
-    if (o.idx) __stcs(o.idx + i, static_cast<int32_t>(e.idx));
+__device__ __forceinline__ void put_bits_idx(const QueryOut &o, int64_t i, uint32_t bits,
+                                             uint32_t idx) {
+    if (o.val) __stcs(reinterpret_cast<unsigned int *>(o.val) + i, bits);
+    if (o.idx) __stcs(o.idx + i, static_cast<int32_t>(idx));
+}
+
+__device__ __forceinline__ void put_result(const QueryOut &o, int64_t i, Entry e, uint32_t mode) {
+    put_bits_idx(o, i, o.val ? entry_bits(e, mode) : 0u, entry_idx(e));
 }
 
 __device__ __forceinline__ void put_invalid(const QueryOut &o, int64_t i) {
@@ -147,7 +135,7 @@ __device__ __forceinline__ void put_invalid(const QueryOut &o, int64_t i) {
 template <bool ALIGNED>
 __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, uint32_t r,
                                                  int lane) {
-    uint64_t best = ~0ull;
+    Entry best = kEntryNone;
     const int64_t al = v.off + l, ar = v.off + r;
     if (ALIGNED) {
         for (int64_t p = (al & ~int64_t(3)) + 4 * lane; p <= ar; p += 128) {
@@ -166,27 +154,21 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const int64_t g = p + c;
-                if (g >= al && g <= ar) {
-                    const uint64_t k = (static_cast<uint64_t>(key_of(b[c], v.kmode)) << 32) |
-                                       static_cast<uint32_t>(g - v.off);
-                    best = k < best ? k : best;
-                }
+                if (g >= al && g <= ar)
+                    best = better(best, make_entry(b[c], static_cast<uint32_t>(g - v.off), v.kmode));
             }
         }
     } else {
-        for (int64_t g = al + lane; g <= ar; g += 32) {
-            const uint64_t k = (static_cast<uint64_t>(key_of(ld_u1(v.A + g), v.kmode)) << 32) |
-                               static_cast<uint32_t>(g - v.off);
-            best = k < best ? k : best;
-        }
+        for (int64_t g = al + lane; g <= ar; g += 32)
+            best = better(best, make_entry(ld_u1(v.A + g), static_cast<uint32_t>(g - v.off), v.kmode));
     }
+    // 64-bit minimum across the warp: the key word first, then the low word
+    // among the lanes that hold that key
     const uint32_t key = static_cast<uint32_t>(best >> 32);
     const uint32_t kmin = __reduce_min_sync(0xffffffffu, key);
     const uint32_t cand = (key == kmin) ? static_cast<uint32_t>(best) : 0xffffffffu;
-    Entry e;
-    e.idx = __reduce_min_sync(0xffffffffu, cand);
-    e.bits = ld_u1(v.A + v.off + e.idx);
-    return e;
+    const uint32_t lo = __reduce_min_sync(0xffffffffu, cand);
+    return (static_cast<uint64_t>(kmin) << 32) | lo;
 }
 
 // Answer queries [q0, q1) of one array with the whole CTA. The loop is
@@ -239,10 +221,10 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
             const bool use_suf = cross || (same && r[k] == bend);
             const bool use_pre = cross || (same && l[k] == bstart);
             scan[k] = same && !use_suf && !use_pre;
-            es[k] = use_suf ? v.suf[l[k]] : entry_max(v.kmode);
-            ep[k] = use_pre ? v.pre[r[k]] : entry_max(v.kmode);
-            ea[k] = entry_max(v.kmode);
-            eb[k] = entry_max(v.kmode);
+            es[k] = use_suf ? v.suf[l[k]] : kEntryNone;
+            ep[k] = use_pre ? v.pre[r[k]] : kEntryNone;
+            ea[k] = kEntryNone;
+            eb[k] = kEntryNone;
             if (cross && rB - lB >= 2u) {
                 const uint32_t lo = lB + 1u, hi = rB - 1u;
                 const int lev = ilog2(hi - lo + 1u);
@@ -265,8 +247,8 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                     continue;
                 }
                 const Entry e = scan[k] ? micro_query<ALIGNED>(v, l[k], r[k])
-                                        : better(better(es[k], ep[k], v.kmode), better(ea[k], eb[k], v.kmode), v.kmode);
-                put_result(o, i, e);
+                                        : better(better(es[k], ep[k]), better(ea[k], eb[k]));
+                put_result(o, i, e, v.kmode);
             }
             return;
         }
@@ -275,7 +257,7 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
             if (act[k] && !scan[k]) {
                 const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
                 if (ok[k])
-                    put_result(o, i, better(better(es[k], ep[k], v.kmode), better(ea[k], eb[k], v.kmode), v.kmode));
+                    put_result(o, i, better(better(es[k], ep[k]), better(ea[k], eb[k])), v.kmode);
                 else
                     put_invalid(o, i);
             }
@@ -290,7 +272,8 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                 const uint32_t rs = __shfl_sync(0xffffffffu, r[k], src);
                 const Entry e = warp_scan_range<ALIGNED>(v, ls, rs, lane);
                 if (lane == src)
-                    put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e);
+                    put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e,
+                               v.kmode);
             }
         }
     }
