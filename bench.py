@@ -193,6 +193,22 @@ CPU_KIND = ("HRMQ restated (oracle/hrmq_port.c: balanced-parentheses RMQ of the 
             "hrmq/RMQRMM64.cpp, ties leftmost), queries on all host threads")
 
 
+TRAFFIC_PROFILE = Path(__file__).resolve().parent / "profiles" / "query_kernel_plain_n1e8_q2e26_lr1.md"
+
+
+def profiled_traffic(q):
+    """DRAM bytes (read + write) per query_kernel launch of q queries, from
+    the ncu capture summarised in TRAFFIC_PROFILE (its line
+    `traffic_bytes_per_query: X`, measured on this workload), or None."""
+    try:
+        for line in TRAFFIC_PROFILE.read_text().splitlines():
+            if line.strip().startswith("traffic_bytes_per_query:"):
+                return float(line.split(":", 1)[1]) * q
+    except OSError:
+        pass
+    return None
+
+
 def cpu_sample_rate(A, Q, target_s=12.0, nt=0):
     """The reference's CPU comparator (HRMQ, restated) on the host cores over
     a bounded random sample of the step's queries; build timed apart."""
@@ -491,6 +507,20 @@ def main():
                               "matches_device_path": bool(ok)}
                 del hQ, hV, hI
             if lr == -1:
+                # random-access ceiling on this index: rmq_probe_gather has the
+                # query kernel's grid, query stream and stores but only its two
+                # random lookups (suf[l], pre[r]) per query
+                gfn = lambda: ix.probe_gather(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+                gms = time_steps(gfn, args.steps, args.warmup, stream, barrier)
+                if world > 1:
+                    tt = torch.tensor([gms], device=dev)
+                    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+                    gms = float(tt.item())
+                res["random_access"] = {
+                    "ceiling_rmq_s": world * q / (gms / 1e3), "ceiling_ms_per_step": gms,
+                    "frac": gms / ms, "kernel": "gather_kernel (rmq_probe_gather)",
+                    "pattern": "per query: 8-B query read, two random 8-B lookups (suf[l], pre[r]) "
+                               "in the 0.8 GB prefix / suffix tables, 8-B result write"}
                 headline = (name, lr, Q, bs)
                 # energy: NVML board power over ~1.5 s of headline steps (outside
                 # the timed region), as the reference's power CSVs
@@ -548,9 +578,11 @@ def main():
         "e2e": h.get("e2e"),
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": profiled_traffic(q),
+                     "traffic_source": TRAFFIC_PROFILE.name,
                      "peak_kind": f"{peak_kind} copy bandwidth",
                      "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
+        "random_access_roofline": h.get("random_access"),
         "clocks": clocks,
         "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
         "energy": h.get("energy"),

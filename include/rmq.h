@@ -207,6 +207,19 @@ int rmq_query_scan(const float *d_vals, int64_t n, const int32_t *d_queries,
                    int64_t q, float *d_val, int32_t *d_idx,
                    rmq_stream_t stream);
 
+/*
+ * Measurement helper, no reference counterpart: the random-access ceiling
+ * of rmq_query on this index. One launch with rmq_query's grid, query
+ * stream and output stores, but per query only the two random 8-byte
+ * lookups of its cross-block case (suffix minimum at l, prefix minimum at r)
+ * and no other work. The outputs are better(suf[l], pre[r]), which is the
+ * range minimum only when l and r lie in the same or in adjacent blocks;
+ * out-of-range l / r are clamped into the array. A benchmark times it
+ * beside rmq_query to state the fraction of this ceiling a query reaches.
+ */
+int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
+                     float *d_val, int32_t *d_idx, rmq_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Batched ragged form: many independent arrays of uneven length, each with
  * its own queries, built and answered by ONE persistent cooperative kernel

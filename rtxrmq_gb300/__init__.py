@@ -134,6 +134,20 @@ class RMQIndex:
         check(load().rmq_query_host(self._h, hptr(queries), q, hptr(out_val), hptr(out_idx),
                                     _stream_handle(stream)))
 
+    def probe_gather(self, queries, out_val=None, out_idx=None, stream=None) -> Tuple:
+        """rmq_probe_gather: the two-lookup random-access ceiling of query()
+        on this index (a measurement helper; its outputs are range minima
+        only for queries whose ends lie in the same or adjacent blocks)."""
+        import torch
+        q = _check_queries(queries)
+        if out_val is None:
+            out_val = torch.empty(q, dtype=getattr(self, "_vdtype", torch.float32), device=queries.device)
+        if out_idx is None:
+            out_idx = torch.empty(q, dtype=torch.int32, device=queries.device)
+        check(load().rmq_probe_gather(self._h, _dptr(queries), q, _dptr(out_val), _dptr(out_idx),
+                                      _stream_handle(stream)))
+        return out_val, out_idx
+
     def save(self, path, stream=None) -> None:
         """Write the index (not the values) to ``path`` (rmq_save)."""
         check(load().rmq_save(self._h, str(path).encode(), _stream_handle(stream)))

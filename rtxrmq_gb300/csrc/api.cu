@@ -240,6 +240,35 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float 
     return RMQ_OK;
 }
 
+int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float *d_val,
+                     int32_t *d_idx, rmq_stream_t stream) {
+    g_err[0] = '\0';
+    if (!h) return set_error(RMQ_EINVAL, "rmq_probe_gather: handle is NULL");
+    if (q < 0) return set_error(RMQ_EINVAL, "rmq_probe_gather: q=%lld < 0", (long long)q);
+    if (q == 0) return RMQ_OK;
+    if (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8 != 0)
+        return set_error(RMQ_EINVAL, "rmq_probe_gather: d_queries NULL or not 8-byte aligned");
+    if (!d_val && !d_idx) return set_error(RMQ_EINVAL, "rmq_probe_gather: both outputs are NULL");
+    if ((d_val && reinterpret_cast<uintptr_t>(d_val) % 4) ||
+        (d_idx && reinterpret_cast<uintptr_t>(d_idx) % 4))
+        return set_error(RMQ_EINVAL, "rmq_probe_gather: outputs not 4-byte aligned");
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    if (dev.device != h->device)
+        return set_error(RMQ_EINVAL, "rmq_probe_gather: handle built on device %d, current is %d",
+                         h->device, dev.device);
+    QueryArgs a;
+    a.Q = reinterpret_cast<const int2 *>(d_queries);
+    a.q = q;
+    a.val = d_val;
+    a.idx = d_idx;
+    a.invalid = nullptr;
+    cudaError_t err = launch_probe_gather(h->plan, a, dev, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_probe_gather: launch");
+    return RMQ_OK;
+}
+
 // True when p is device (or managed) memory of the current context.
 static bool is_device_memory(const void *p) {
     cudaPointerAttributes at;

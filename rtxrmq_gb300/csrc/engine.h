@@ -80,6 +80,8 @@ cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInf
                          cudaStream_t s);
 struct V1View;
 V1View view_of(const BuildPlan &p);
+cudaError_t launch_probe_gather(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,
+                                cudaStream_t s);
 cudaError_t launch_query_scan(const float *A, uint32_t n, const QueryArgs &a,
                               const DeviceInfo &dev, cudaStream_t s);
 

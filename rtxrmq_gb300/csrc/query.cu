@@ -44,6 +44,34 @@ query_kernel(V1View v, QueryOut o, int64_t q) {
     }
 }
 
+// Random-access ceiling of query_kernel (rmq_probe_gather): the same grid,
+// query stream and output stores, but per query only the two random
+// 8-byte lookups suf[l] and pre[r] (no block decision, no table probe, no
+// scan). Its rate bounds what any two-lookup query kernel reaches on this
+// index; its answers are not range minima.
+__global__ void __launch_bounds__(kThreads)
+gather_kernel(V1View v, QueryOut o, int64_t q) {
+    const int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * chunk;
+    for (int64_t c0 = static_cast<int64_t>(blockIdx.x) * chunk; c0 < q; c0 += stride) {
+        int2 qq[kQPT];
+        load_queries<kQPT>(o, c0, c0 + chunk < q ? c0 + chunk : q, qq);
+        Entry e[kQPT];
+#pragma unroll
+        for (int k = 0; k < kQPT; ++k) {
+            // clamped into the array: the probe never reads out of bounds
+            const uint32_t l = min(static_cast<uint32_t>(max(qq[k].x, 0)), v.n - 1u);
+            const uint32_t r = min(static_cast<uint32_t>(max(qq[k].y, 0)), v.n - 1u);
+            e[k] = better(v.suf[l], v.pre[r]);
+        }
+#pragma unroll
+        for (int k = 0; k < kQPT; ++k) {
+            const int64_t i = c0 + threadIdx.x + static_cast<int64_t>(k) * kThreads;
+            if (i < q) put_result(o, i, e[k], v.kmode);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads)
 scan_kernel(const float *__restrict__ A, uint32_t n, QueryOut o, int64_t q) {
     const int64_t stride = static_cast<int64_t>(gridDim.x) * kThreads;
@@ -68,6 +96,7 @@ scan_kernel(const float *__restrict__ A, uint32_t n, QueryOut o, int64_t q) {
 }
 
 int g_query_per_sm[2] = {0, 0};
+int g_gather_per_sm = 0;
 int g_scan_per_sm = 0;
 
 template <typename K>
@@ -129,6 +158,22 @@ cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInf
         query_kernel<false><<<grid_size(a.q, kThreads * kQPT, g_query_per_sm[0], dev), kThreads,
                               0, s>>>(v, o, a.q);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probe_gather(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,
+                                cudaStream_t s) {
+    if (a.q <= 0) return cudaSuccess;
+    const V1View v = view_of(p);
+    QueryOut o;
+    o.Q = a.Q;
+    o.val = a.val;
+    o.idx = a.idx;
+    o.invalid = nullptr;
+    cudaError_t err = occupancy(gather_kernel, &g_gather_per_sm);
+    if (err != cudaSuccess) return err;
+    gather_kernel<<<grid_size(a.q, kThreads * kQPT, g_gather_per_sm, dev), kThreads, 0, s>>>(v, o,
+                                                                                            a.q);
     return cudaGetLastError();
 }
 

@@ -404,3 +404,31 @@ def test_key_modes(cuda, native, dtype, op, micro):
             i, v = i.cpu().numpy(), v.cpu().numpy()
         np.testing.assert_array_equal(i, ei)
         np.testing.assert_array_equal(v.view(np.uint32), A[ei].view(np.uint32))
+
+
+def test_probe_gather(cuda, native, oracle_lib):
+    """rmq_probe_gather (the random-access ceiling the bench times beside
+    rmq_query) reads suf[l] and pre[r] only: exact for queries whose ends lie
+    in adjacent blocks, clamped (no fault, no error) for out-of-range ones."""
+    import torch
+
+    import oracle
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(11)
+    n, bs = 100_000, 1000
+    A = rng.integers(0, 64, n).astype(np.float32)  # many ties
+    lb = rng.integers(0, n // bs - 1, 20_000)
+    l = lb * bs + rng.integers(0, bs, lb.size)
+    r = (lb + 1) * bs + rng.integers(0, bs, lb.size)
+    Q = np.stack([l, r], axis=1).astype(np.int32)
+    ev, ei = oracle.base_val(A, Q), oracle.base_idx(A, Q)
+    dA = torch.from_numpy(A).to(cuda)
+    with R.RMQIndex(dA, bs) as ix:
+        v, i = ix.probe_gather(torch.from_numpy(Q).to(cuda))
+        bad = torch.tensor([[-5, 3], [7, n + 100], [n + 1, n + 2]], dtype=torch.int32, device=cuda)
+        vb, ib = ix.probe_gather(bad)
+        torch.cuda.synchronize()
+        assert ix.invalid_count() == 0
+    assert_matches(A, Q, v.cpu().numpy(), i.cpu().numpy(), ev, ei)
+    ib = ib.cpu().numpy()
+    assert ((ib >= 0) & (ib < n)).all()
