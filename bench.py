@@ -184,7 +184,9 @@ def time_steps(fn, steps, warmup, stream, barrier):
     t1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    return t0.elapsed_time(t1) / steps  # ms per step
+    from rtxrmq_gb300.replicas import max_over_ranks
+    # ms per step, the maximum over ranks under torchrun (replicas)
+    return max_over_ranks(t0.elapsed_time(t1) / steps, torch.cuda.current_device())
 
 
 # ---------------------------------------------------------------- CPU side
@@ -334,12 +336,13 @@ def bench_batched(args, dev, stream, barrier):
         del g
     with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, None) as b:
         dms = time_steps(lambda: b.run(dV, dQ, ov, oi), args.steps, 1, stream, barrier)
-    q = w.total_q
-    res.update({"batched_graph_rmq_s": q / (gms / 1e3), "batched_graph_ms": gms,
-                "batched_rmq_s": q / (ms / 1e3), "batched_ms": ms,
-                "per_array_rmq_s": q / (pms / 1e3), "per_array_ms": pms,
+    from rtxrmq_gb300.replicas import job_rate, world
+    q, nr = w.total_q, world()[1]
+    res.update({"batched_graph_rmq_s": job_rate(q, nr, gms), "batched_graph_ms": gms,
+                "batched_rmq_s": job_rate(q, nr, ms), "batched_ms": ms,
+                "per_array_rmq_s": job_rate(q, nr, pms), "per_array_ms": pms,
                 "speedup_vs_per_array": pms / gms,
-                "default_bs_rmq_s": q / (dms / 1e3),
+                "default_bs_rmq_s": job_rate(q, nr, dms),
                 "per_array_matches_batched": match,
                 "launches_per_step": {"batched": 1, "per_array": "one build + level + query "
                                       "launch sequence per array"}})
@@ -380,6 +383,7 @@ def bench_autograd(args, dev, stream, barrier):
     gf = graph_of(fwd, stream)
     xg.grad = None
     gb = graph_of(fwd_bwd, stream)
+    from rtxrmq_gb300.replicas import job_rate, world
     fms = time_steps(gf.replay, args.steps, args.warmup, stream, barrier)
     bms = time_steps(gb.replay, args.steps, args.warmup, stream, barrier)
     # full-size check of the gradient against an FP64 scatter of the same argmins
@@ -401,7 +405,7 @@ def bench_autograd(args, dev, stream, barrier):
                        "0.4 ln len, 0.5), grad_out N(0,1)",
            "elements": d.span, "queries": q, "bucket_bs": {str(b): v for b, v in enumerate(cfg) if v},
            "fwd_ms": fms, "fwd_bwd_ms": bms, "fwd_bwd_over_fwd": bms / fms,
-           "fwd_rmq_s": q / (fms / 1e3), "fwd_bwd_rmq_s": q / (bms / 1e3),
+           "fwd_rmq_s": job_rate(q, world()[1], fms), "fwd_bwd_rmq_s": job_rate(q, world()[1], bms),
            "graph_captured": True, "grad_max_rel_err_vs_fp64": rel, "grad_zero_elsewhere": zero_ok}
     del gf, gb, x, xg, dQ, go
     torch.cuda.empty_cache()
@@ -421,6 +425,7 @@ def main():
     import torch.distributed as dist
 
     import rtxrmq_gb300 as R
+    from rtxrmq_gb300.replicas import job_rate, rank_seed
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -448,7 +453,7 @@ def main():
     with sampler:
         for name, lr in modes:
             # replicas: each rank answers its own query set (seeded by rank)
-            Q = R.gen_queries(q, n, lr, SEED + 1 + 1000 * rank + (0 if lr == -1 else 17 * abs(lr)))
+            Q = R.gen_queries(q, n, lr, rank_seed(SEED, rank, lr))
             dQ = torch.from_numpy(Q).to(dev)
             sweep = {}
             best = None
@@ -468,12 +473,8 @@ def main():
             construction_ms = (time.perf_counter() - t) * 1e3
             fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
             ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
-            if world > 1:
-                tt = torch.tensor([ms], device=dev)
-                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-                ms = float(tt.item())
             alg_bytes, mix = algorithmic_bytes(Q, n, bs, 8)
-            res = {"value": world * q / (ms / 1e3), "ms_per_step": ms, "bs": bs,
+            res = {"value": job_rate(q, world, ms), "ms_per_step": ms, "bs": bs,
                    "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
                    "construction_ms": construction_ms, "mix": mix,
                    "alg_bytes_per_step": alg_bytes,
@@ -491,16 +492,12 @@ def main():
                     ix.query_host(hQ, hV, hI)
 
                 e2e_ms = time_steps(e2e, args.steps, args.warmup, stream, barrier)
-                if world > 1:
-                    tt = torch.tensor([e2e_ms], device=dev)
-                    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-                    e2e_ms = float(tt.item())
-                torch.cuda.synchronize()
+                    torch.cuda.synchronize()
                 ix.query(dQ, out_val=out_v, out_idx=out_i)
                 torch.cuda.synchronize()
                 ok = (np.array_equal(hI.numpy(), out_i.cpu().numpy()) and
                       np.array_equal(hV.numpy().view(np.uint32), out_v.cpu().numpy().view(np.uint32)))
-                res["e2e"] = {"value": world * q / (e2e_ms / 1e3), "unit": "RMQ/s",
+                res["e2e"] = {"value": job_rate(q, world, e2e_ms), "unit": "RMQ/s",
                               "h2d_bytes_per_step": int(Q.nbytes),
                               "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
                               "ms_per_step": e2e_ms, "path": "rmq_query_host, pinned host buffers read and written in place",
@@ -512,12 +509,8 @@ def main():
                 # random lookups (suf[l], pre[r]) per query
                 gfn = lambda: ix.probe_gather(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
                 gms = time_steps(gfn, args.steps, args.warmup, stream, barrier)
-                if world > 1:
-                    tt = torch.tensor([gms], device=dev)
-                    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-                    gms = float(tt.item())
-                res["random_access"] = {
-                    "ceiling_rmq_s": world * q / (gms / 1e3), "ceiling_ms_per_step": gms,
+                    res["random_access"] = {
+                    "ceiling_rmq_s": job_rate(q, world, gms), "ceiling_ms_per_step": gms,
                     "frac": gms / ms, "kernel": "gather_kernel (rmq_probe_gather)",
                     "pattern": "per query: 8-B query read, two random 8-B lookups (suf[l], pre[r]) "
                                "in the 0.8 GB prefix / suffix tables, 8-B result write"}
