@@ -41,15 +41,17 @@ def plain_data(cuda, native):
     return A, torch.from_numpy(A).to(cuda)
 
 
-@pytest.mark.parametrize("lr", [-1, -2, -3, 1024])
-def test_plain_n1e8_q2e26(cuda, native, oracle_lib, plain_data, lr):
+# the block sizes the benchmark's sweep settles on per mode, and 4096
+@pytest.mark.parametrize("lr,bs", [(-1, 4096), (-1, 1 << 16), (-2, 4096), (-2, 1 << 14),
+                                   (-3, 4096), (-3, 1024), (1024, 4096), (1024, 1024)])
+def test_plain_n1e8_q2e26(cuda, native, oracle_lib, plain_data, lr, bs):
     import torch
 
     import rtxrmq_gb300 as R
     A, dA = plain_data
     Q = R.gen_queries(1 << 26, len(A), lr, 1322)
     dQ = torch.from_numpy(Q).to(cuda)
-    with R.RMQIndex(dA, 4096) as ix:
+    with R.RMQIndex(dA, bs) as ix:
         v, i = ix.query(dQ)
         torch.cuda.synchronize()
         assert ix.invalid_count() == 0
@@ -81,4 +83,35 @@ def test_tie_heavy_n2e27_q2e26(cuda, native, oracle_lib, length):
     if length <= 1 << 10:
         sampled_exact(oracle_lib, A, Q, v, i, 1 << 16, 10, base=True)
     del dA, dQ
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("bucket_bs", [None, [256] * 32, [64] * 17 + [256] * 15])
+def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs):
+    """Batched ragged configuration at full size (4096 arrays, lengths
+    round(2^U) with U ~ U[8,22], 2^26 queries): every answer's properties,
+    and a sample exactly against BASE on the shared value buffer (a query
+    (l, r) of the array at offset o is the global query (o+l, o+r))."""
+    import torch
+
+    from rtxrmq_gb300 import workloads as W
+    from rtxrmq_gb300.batch import RMQBatch
+    w = W.ragged()
+    dV = torch.from_numpy(w.values).to(cuda)
+    dQ = torch.from_numpy(w.queries).to(cuda)
+    with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, bucket_bs) as b:
+        v, i = b.run(dV, dQ)
+        torch.cuda.synchronize()
+        assert b.invalid_count() == 0
+    v, i = v.cpu().numpy(), i.cpu().numpy().astype(np.int64)
+    off = np.repeat(w.starts, w.qcounts)
+    G = w.queries.astype(np.int64) + off[:, None]
+    gi = i + off
+    assert (gi >= G[:, 0]).all() and (gi <= G[:, 1]).all(), "index outside its range"
+    np.testing.assert_array_equal(w.values[gi].view(np.uint32), v.view(np.uint32))
+    s = np.random.default_rng(12).integers(0, len(G), 1 << 14)
+    ev, ei = oracle_lib.base_val(w.values, G[s]), oracle_lib.base_idx(w.values, G[s])
+    np.testing.assert_array_equal(gi[s], ei)
+    np.testing.assert_array_equal(v[s].view(np.uint32), ev.view(np.uint32))
+    del dV, dQ
     torch.cuda.empty_cache()
