@@ -27,9 +27,11 @@ struct rmq_handle {
     // their chunks on the shared staging buffers
     std::mutex *host_mu;
     void *stage;
-    cudaStream_t ks;           // chunk kernels (and query copies), in order
+    cudaStream_t hs;           // query copies into staging
+    cudaStream_t ks;           // chunk kernels, in order
     cudaStream_t cs;           // result copies, each after its chunk's kernel
     cudaEvent_t ev_start;
+    cudaEvent_t h_done[3];     // per staging slot: queries copied in
     cudaEvent_t k_done[3];     // per staging slot: kernel finished
     cudaEvent_t c_done[3];     // per staging slot: results copied out
     cudaEvent_t ev_end;
@@ -307,23 +309,30 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
     if (q == 0) return RMQ_OK;
     if (!h_queries) return set_error(RMQ_EINVAL, "rmq_query_host: h_queries is NULL");
     if (!h_val && !h_idx) return set_error(RMQ_EINVAL, "rmq_query_host: both outputs are NULL");
-    // RTXRMQ_HOST_STAGED=1 takes the staged path even for addressable
-    // buffers (it is otherwise only reached on systems without page-locked
-    // or pageable access; the tests use it to cover that path everywhere)
+    // RTXRMQ_HOST_STAGED=1 takes the staged path for every buffer, as on a
+    // system where the device cannot address host memory (the tests use it
+    // to cover that path everywhere). RTXRMQ_HOST_MODE=<m> moves addressable
+    // host buffers to staging anyway: bit 0 the results, bit 1 the queries.
     const char *force = std::getenv("RTXRMQ_HOST_STAGED");
     const bool forced = force && force[0] == '1';
-    if (!forced) {
-        // every buffer addressable by the device (device memory, page-locked
-        // host memory, or host memory on a system where the device reads
-        // pageable memory): the query kernel reads and writes them in place
-        const void *dq = device_address(h_queries);
-        const void *dv = h_val ? device_address(h_val) : nullptr;
-        const void *di = h_idx ? device_address(h_idx) : nullptr;
-        if (dq && (!h_val || dv) && (!h_idx || di))
-            return rmq_query(h, static_cast<const int32_t *>(dq), q,
-                             static_cast<float *>(const_cast<void *>(dv)),
-                             static_cast<int32_t *>(const_cast<void *>(di)), stream);
-    }
+    const char *mode_s = std::getenv("RTXRMQ_HOST_MODE");
+    const int mode = mode_s ? std::atoi(mode_s) : 0;
+    // device memory, page-locked host memory, or host memory on a system
+    // where the device reads pageable memory: the kernel reads / writes it
+    // in place
+    const int2 *qdev = forced ? nullptr : static_cast<const int2 *>(device_address(h_queries));
+    float *vdev = (forced || !h_val) ? nullptr
+                  : static_cast<float *>(const_cast<void *>(device_address(h_val)));
+    int32_t *idev = (forced || !h_idx) ? nullptr
+                    : static_cast<int32_t *>(const_cast<void *>(device_address(h_idx)));
+    if ((mode & 2) && !is_device_memory(h_queries)) qdev = nullptr;
+    if ((mode & 1) && h_val && !is_device_memory(h_val)) vdev = nullptr;
+    if ((mode & 1) && h_idx && !is_device_memory(h_idx)) idev = nullptr;
+    const bool v_stage = h_val && !vdev;
+    const bool i_stage = h_idx && !idev;
+    if (qdev && !v_stage && !i_stage)
+        return rmq_query(h, reinterpret_cast<const int32_t *>(qdev), q, vdev, idev, stream);
+
     DeviceInfo dev;
     int rc = device_info(&dev);
     if (rc) return rc;
@@ -335,10 +344,12 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
     cudaError_t err = cudaSuccess;
     if (!hm->stage) {
         err = cudaMalloc(&hm->stage, kHostStreams * kHostChunk * 16);
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->hs, cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->ks, cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->cs, cudaStreamNonBlocking);
         for (int s = 0; s < kHostStreams && err == cudaSuccess; ++s) {
-            err = cudaEventCreateWithFlags(&hm->k_done[s], cudaEventDisableTiming);
+            err = cudaEventCreateWithFlags(&hm->h_done[s], cudaEventDisableTiming);
+            if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->k_done[s], cudaEventDisableTiming);
             if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->c_done[s], cudaEventDisableTiming);
         }
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->ev_start, cudaEventDisableTiming);
@@ -346,51 +357,54 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
         if (err != cudaSuccess) return cuda_fail(err, "rmq_query_host: staging set-up");
     }
     err = cudaEventRecord(hm->ev_start, stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->hs, hm->ev_start, 0);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->ks, hm->ev_start, 0);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->cs, hm->ev_start, 0);
-    // Queries the device can address are read in place by the kernel (on
-    // Grace-Blackwell at no cost to the kernel); others are copied into
-    // staging. Results go to device staging and are copied out by the copy
-    // engines (kernel stores into host memory slow the kernel's lookups).
-    // The chunk kernels run in order on one stream; each chunk's result copy
-    // follows on a second stream, overlapping the next chunks' kernels; a
-    // staging slot is reused only after its previous copy-out finished.
-    const int2 *qdev = forced ? nullptr : static_cast<const int2 *>(device_address(h_queries));
-    const bool val_dev = h_val && is_device_memory(h_val);
-    const bool idx_dev = h_idx && is_device_memory(h_idx);
+    // Chunks of kHostChunk queries over kHostStreams staging slots, three
+    // streams: query copies in (hs), the chunk kernels in order (ks), result
+    // copies out (cs), each chunk's steps ordered by per-slot events; a slot
+    // is reused only when the kernel has read its queries and the copy-out
+    // has read its results.
     for (int64_t c = 0, i = 0; c < q && err == cudaSuccess; c += kHostChunk, ++i) {
         const int b = static_cast<int>(i % kHostStreams);
         const int64_t m = q - c < kHostChunk ? q - c : kHostChunk;
         char *base = static_cast<char *>(hm->stage) + b * kHostChunk * 16;
-        if (i >= kHostStreams) err = cudaStreamWaitEvent(hm->ks, hm->c_done[b], 0);
-        if (err != cudaSuccess) break;
         QueryArgs a;
         if (qdev) {
             a.Q = qdev + c;
         } else {
             int32_t *dq = reinterpret_cast<int32_t *>(base);
-            err = cudaMemcpyAsync(dq, h_queries + 2 * c, m * 8, cudaMemcpyHostToDevice, hm->ks);
+            if (i >= kHostStreams) err = cudaStreamWaitEvent(hm->hs, hm->k_done[b], 0);
+            if (err == cudaSuccess)
+                err = cudaMemcpyAsync(dq, h_queries + 2 * c, m * 8, cudaMemcpyHostToDevice, hm->hs);
+            if (err == cudaSuccess) err = cudaEventRecord(hm->h_done[b], hm->hs);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->ks, hm->h_done[b], 0);
             if (err != cudaSuccess) break;
             a.Q = reinterpret_cast<const int2 *>(dq);
         }
-        float *dv = !h_val ? nullptr
-                    : val_dev ? h_val + c : reinterpret_cast<float *>(base + kHostChunk * 8);
+        if ((v_stage || i_stage) && i >= kHostStreams)
+            err = cudaStreamWaitEvent(hm->ks, hm->c_done[b], 0);
+        if (err != cudaSuccess) break;
+        float *dv = !h_val ? nullptr : v_stage ? reinterpret_cast<float *>(base + kHostChunk * 8) : vdev + c;
         int32_t *di = !h_idx ? nullptr
-                      : idx_dev ? h_idx + c : reinterpret_cast<int32_t *>(base + kHostChunk * 12);
+                      : i_stage ? reinterpret_cast<int32_t *>(base + kHostChunk * 12) : idev + c;
         a.q = m;
         a.val = dv;
         a.idx = di;
         a.invalid = h->invalid;
         err = launch_query(h->plan, a, dev, hm->ks);
         if (err == cudaSuccess) err = cudaEventRecord(hm->k_done[b], hm->ks);
-        if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->cs, hm->k_done[b], 0);
-        if (err == cudaSuccess && h_val && !val_dev)
-            err = cudaMemcpyAsync(h_val + c, dv, m * 4, cudaMemcpyDeviceToHost, hm->cs);
-        if (err == cudaSuccess && h_idx && !idx_dev)
-            err = cudaMemcpyAsync(h_idx + c, di, m * 4, cudaMemcpyDeviceToHost, hm->cs);
-        if (err == cudaSuccess) err = cudaEventRecord(hm->c_done[b], hm->cs);
+        if (err == cudaSuccess && (v_stage || i_stage)) {
+            err = cudaStreamWaitEvent(hm->cs, hm->k_done[b], 0);
+            if (err == cudaSuccess && v_stage)
+                err = cudaMemcpyAsync(h_val + c, dv, m * 4, cudaMemcpyDeviceToHost, hm->cs);
+            if (err == cudaSuccess && i_stage)
+                err = cudaMemcpyAsync(h_idx + c, di, m * 4, cudaMemcpyDeviceToHost, hm->cs);
+            if (err == cudaSuccess) err = cudaEventRecord(hm->c_done[b], hm->cs);
+        }
     }
-    // `stream` continues when both internal streams are done
+    // `stream` continues when the kernel and copy-out streams are done (the
+    // query copies precede their kernels)
     if (err == cudaSuccess) err = cudaEventRecord(hm->ev_end, hm->ks);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(stream, hm->ev_end, 0);
     if (err == cudaSuccess) err = cudaEventRecord(hm->ev_end, hm->cs);
@@ -404,6 +418,10 @@ int rmq_free(rmq_handle_t *h) {
     if (!h) return RMQ_OK;
     cudaError_t err = cudaSuccess;
     if (h->stage) {
+        if (h->hs) {
+            cudaStreamSynchronize(h->hs);
+            cudaStreamDestroy(h->hs);
+        }
         if (h->ks) {
             cudaStreamSynchronize(h->ks);
             cudaStreamDestroy(h->ks);
@@ -413,6 +431,7 @@ int rmq_free(rmq_handle_t *h) {
             cudaStreamDestroy(h->cs);
         }
         for (int s = 0; s < kHostStreams; ++s) {
+            if (h->h_done[s]) cudaEventDestroy(h->h_done[s]);
             if (h->k_done[s]) cudaEventDestroy(h->k_done[s]);
             if (h->c_done[s]) cudaEventDestroy(h->c_done[s]);
         }

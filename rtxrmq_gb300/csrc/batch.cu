@@ -38,7 +38,7 @@ namespace cg = cooperative_groups;
 namespace rmq {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kBuildThreads;  // phase A runs the unit builder
 constexpr int kQPT = 2;
 constexpr uint32_t kQueryChunk = 2048;  // queries per query item
 constexpr uint32_t kLevelChunk = 4096;  // sparse-table entries per level item

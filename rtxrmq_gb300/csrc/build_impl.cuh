@@ -28,13 +28,26 @@
 
 namespace rmq {
 
-constexpr int kBuildThreads = 256;
-constexpr int kBuildEPT = 16;                           // elements per thread per tile
-constexpr int kBuildTile = kBuildThreads * kBuildEPT;   // 4096
+// Tile geometry (compile-time tunables): threads per builder CTA and
+// consecutive elements per thread (a power of two, multiple of 4).
+#ifndef RMQ_BUILD_THREADS
+#define RMQ_BUILD_THREADS 256
+#endif
+#ifndef RMQ_BUILD_EPT
+#define RMQ_BUILD_EPT 16
+#endif
+constexpr int kBuildThreads = RMQ_BUILD_THREADS;
+constexpr int kBuildEPT = RMQ_BUILD_EPT;                // elements per thread per tile
+constexpr int kBuildTile = kBuildThreads * kBuildEPT;   // 4096 by default
 constexpr int kBuildWarps = kBuildThreads / 32;
-constexpr uint32_t kUnitTarget = 4096;                  // elements per multi-block unit
-constexpr int kStageEntries = kBuildTile + kBuildTile / 16;
-constexpr int kWarpSlots = 2 * kBuildWarps;             // shared words for the CTA scans
+constexpr uint32_t kUnitTarget = kBuildTile;            // elements per multi-block unit
+// staging: one padding entry after every thread's kBuildEPT entries
+constexpr int kStageEntries = kBuildTile + kBuildTile / kBuildEPT;
+static_assert(kBuildEPT % 4 == 0 && (kBuildEPT & (kBuildEPT - 1)) == 0, "kBuildEPT");
+constexpr int kMaxStreamTiles = 64;                     // blocks up to 64 tiles: two-phase build
+// shared words: CTA scans (2 x warps), per-tile minima and suffix carries of
+// a multi-tile block (2 x kMaxStreamTiles)
+constexpr int kWarpSlots = 2 * kBuildWarps + 2 * kMaxStreamTiles;
 
 struct UnitLayout {
     uint32_t G;           // blocks per unit
@@ -231,7 +244,7 @@ __device__ __forceinline__ void build_unit_tiles(const UnitJob &J, uint32_t u, E
                 const uint32_t e = threadIdx.x + k * kBuildThreads;
                 const int64_t g = t0 + e;
                 if (g >= a_lo && g < a_hi) {
-                    const Entry en = stage[e + (e >> 4)];
+                    const Entry en = stage[e + e / kBuildEPT];
                     const uint32_t local = static_cast<uint32_t>(g - J.off);
                     st_entry(out + local, en);
                     if (!suffix) {
@@ -369,7 +382,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         const uint32_t e = threadIdx.x + k * kBuildThreads;
         const uint32_t ul = e - static_cast<uint32_t>(lead);
         if (ul < ulen) {
-            st_entry(J.pre + ustart + ul, stage[e + (e >> 4)]);
+            st_entry(J.pre + ustart + ul, stage[e + e / kBuildEPT]);
         }
     }
     {
@@ -378,7 +391,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         for (uint32_t b = threadIdx.x; b < nblk; b += kBuildThreads) {
             const uint32_t last = min((b + 1u) * J.bs, ulen) - 1u;
             const uint32_t e = last + static_cast<uint32_t>(lead);
-            J.bmin[u * G + b] = stage[e + (e >> 4)];
+            J.bmin[u * G + b] = stage[e + e / kBuildEPT];
         }
     }
     __syncthreads();
@@ -402,11 +415,141 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         const uint32_t e = threadIdx.x + k * kBuildThreads;
         const uint32_t ul = e - static_cast<uint32_t>(lead);
         if (ul < ulen) {
-            st_entry(J.suf + ustart + ul, stage[e + (e >> 4)]);
+            st_entry(J.suf + ustart + ul, stage[e + e / kBuildEPT]);
         }
     }
     // The next unit's first shared-memory writes (s_warp, stage) come after
     // a barrier every thread reaches only when it has finished these reads.
+}
+
+// Block of more than one tile (one block per unit, up to kMaxStreamTiles
+// tiles). Phase 1 streams the block once for its per-tile minima; the
+// suffix carry of each tile (minimum of the tiles after it) follows from
+// them. Phase 2 streams it again (mostly from L2) and builds every tile as a
+// one-tile unit, with the running prefix carry and the tile's suffix carry
+// folded into the CTA scan's results. Elements are combined directly as
+// index entries.
+template <bool ALIGNED, uint32_t MODE>
+__device__ __forceinline__ void build_unit_stream(const UnitJob &J, uint32_t u, Entry *stage,
+                                                  uint64_t *s_warp) {
+    const uint32_t ustart = u * J.bs;
+    const uint32_t ulen = min(ustart + J.bs, J.n) - ustart;
+    const int64_t a_lo = J.off + ustart;
+    const int64_t t_first = ALIGNED ? (a_lo & ~int64_t(3)) : a_lo;
+    const uint32_t lead = static_cast<uint32_t>(a_lo - t_first);
+    const uint32_t ntiles = (lead + ulen + kBuildTile - 1) / kBuildTile;
+    uint64_t *s_tmin = s_warp + 2 * kBuildWarps;
+    uint64_t *s_sufc = s_tmin + kMaxStreamTiles;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    constexpr bool kFloat = (MODE == kFloatMin || MODE == kFloatMax);
+
+    // this thread's 16 elements of tile t as entries (kEntryNone outside the block)
+    auto load_tile = [&](uint32_t t, Entry (&c)[kBuildEPT]) {
+        const int64_t base = t_first + static_cast<int64_t>(t) * kBuildTile +
+                             static_cast<int64_t>(threadIdx.x) * kBuildEPT;
+        const uint32_t ul0 = t * kBuildTile + threadIdx.x * kBuildEPT - lead;  // may wrap
+        uint32_t bits[kBuildEPT];
+        if (ALIGNED && base + kBuildEPT <= J.limit) {
+#pragma unroll
+            for (int v = 0; v < kBuildEPT / 4; ++v) {
+                const uint4 f = ld_u4(J.A + base + 4 * v);
+                bits[4 * v + 0] = f.x;
+                bits[4 * v + 1] = f.y;
+                bits[4 * v + 2] = f.z;
+                bits[4 * v + 3] = f.w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < kBuildEPT; ++j)
+                bits[j] = (ul0 + j < ulen) ? ld_u1(J.A + base + j) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kBuildEPT; ++j) {
+            const uint32_t ul = ul0 + j;
+            const uint32_t nz = (kFloat && bits[j] == 0x80000000u) ? 1u : 0u;
+            const Entry e = (static_cast<uint64_t>(key_of(bits[j], MODE)) << 32) |
+                            ((ustart + ul) << 1) | nz;
+            c[j] = ul < ulen ? e : kEntryNone;
+        }
+    };
+
+    // phase 1: per-tile minima (warp minima in alternating slots, one barrier a tile)
+#pragma unroll 1
+    for (uint32_t t = 0; t < ntiles; ++t) {
+        Entry c[kBuildEPT];
+        load_tile(t, c);
+        uint64_t m = c[0];
+#pragma unroll
+        for (int j = 1; j < kBuildEPT; ++j) m = umin64(m, c[j]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = umin64(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) s_warp[(t & 1u) * kBuildWarps + warp] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t tm = s_warp[(t & 1u) * kBuildWarps];
+#pragma unroll
+            for (int w = 1; w < kBuildWarps; ++w) tm = umin64(tm, s_warp[(t & 1u) * kBuildWarps + w]);
+            s_tmin[t] = tm;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t acc = kEntryNone;
+        for (uint32_t t = ntiles; t-- > 0;) {
+            s_sufc[t] = acc;
+            acc = umin64(acc, s_tmin[t]);
+        }
+        J.bmin[u] = acc;  // block minimum
+    }
+    __syncthreads();
+
+    // phase 2: every tile as a one-tile unit with carries
+    uint64_t carry = kEntryNone;  // minimum of the tiles before t
+#pragma unroll 1
+    for (uint32_t t = 0; t < ntiles; ++t) {
+        Entry c[kBuildEPT];
+        load_tile(t, c);
+        uint64_t agg = c[0];
+#pragma unroll
+        for (int j = 1; j < kBuildEPT; ++j) agg = umin64(agg, c[j]);
+        uint64_t ex_p, ex_s;
+        cta_exclusive_min2(agg, agg, s_warp, ex_p, ex_s);
+        ex_p = umin64(ex_p, carry);
+        ex_s = umin64(ex_s, s_sufc[t]);
+        carry = umin64(carry, s_tmin[t]);
+        const int64_t tile_ul = static_cast<int64_t>(t) * kBuildTile - lead;  // offset of tile entry 0
+
+        uint64_t run = ex_p;
+#pragma unroll
+        for (int j = 0; j < kBuildEPT; ++j) {
+            run = umin64(run, c[j]);
+            stage[threadIdx.x * (kBuildEPT + 1) + j] = run;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < kBuildEPT; ++k) {
+            const uint32_t e = threadIdx.x + k * kBuildThreads;
+            const uint32_t ul = static_cast<uint32_t>(tile_ul + e);
+            if (ul < ulen) st_entry(J.pre + ustart + ul, stage[e + e / kBuildEPT]);
+        }
+        __syncthreads();
+        run = ex_s;
+#pragma unroll
+        for (int j = kBuildEPT - 1; j >= 0; --j) {
+            run = umin64(run, c[j]);
+            stage[threadIdx.x * (kBuildEPT + 1) + j] = run;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < kBuildEPT; ++k) {
+            const uint32_t e = threadIdx.x + k * kBuildThreads;
+            const uint32_t ul = static_cast<uint32_t>(tile_ul + e);
+            if (ul < ulen) st_entry(J.suf + ustart + ul, stage[e + e / kBuildEPT]);
+        }
+        // the next tile's first shared writes (s_warp in its CTA scan, then
+        // stage) follow a barrier that every thread reaches after these reads
+    }
 }
 
 // Build unit `u`: one-tile units with the single-pass builder, others with
@@ -420,6 +563,10 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
             build_unit_tile<ALIGNED, MODE, true>(J, u, stage, s_warp);
         else
             build_unit_tile<ALIGNED, MODE, false>(J, u, stage, s_warp);
+    } else if (J.U.G == 1 &&
+               (static_cast<uint32_t>(J.off + u * J.bs - t0) + min(J.bs, J.n - u * J.bs) +
+                kBuildTile - 1) / kBuildTile <= static_cast<uint32_t>(kMaxStreamTiles)) {
+        build_unit_stream<ALIGNED, MODE>(J, u, stage, s_warp);
     } else {
         build_unit_tiles<ALIGNED, MODE>(J, u, stage, s_warp);
     }

@@ -88,7 +88,7 @@ def test_config_small_range(cuda, native, oracle_lib, bs, micro):
 
 @pytest.mark.parametrize("micro", [True, False])
 @pytest.mark.parametrize("lr", [-1, -2, -3, 1, 32, 1024, 65536])
-@pytest.mark.parametrize("bs", [1 << 10, 1 << 13, 1 << 16, 12207, 4000])
+@pytest.mark.parametrize("bs", [1 << 10, 1 << 13, 1 << 16, 12207, 4000, 1 << 18, 1 << 20])
 def test_length_modes_medium(cuda, native, oracle_lib, lr, bs, micro):
     """n=2^22: every length mode and block-size class; oracle = the CPU
     restatement of RTX_blocks (exact, O(bs + nb) per query)."""
