@@ -47,31 +47,75 @@ __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
         cur[j] = better(prev[j], prev[j + half]);
 }
 
-// Sub-block level, one warp per 32-element micro-block (lane = element):
-// in-micro-block prefix and suffix minima by warp shuffles, written with
-// coalesced 256-byte stores, and the micro-block minimum (suffix minimum at
+// Sub-block level: 8 lanes per 32-element micro-block, 4 consecutive
+// elements per lane (one 16-byte load), 4 micro-blocks per warp. Each lane
+// scans its 4 elements both ways, then the 8 lanes of a micro-block scan
+// their totals with width-8 shuffles; results are written as two 16-byte
+// stores per lane and array, and the micro-block minimum (suffix minimum at
 // its first element) as level 0 of the micro table.
 __global__ void __launch_bounds__(256)
 micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entry *mpre,
-                  Entry *msuf, Entry *mst0, uint32_t mode) {
+                  Entry *msuf, Entry *mst0, uint32_t mode, bool aligned) {
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t sub = lane & 7u;        // lane within its micro-block
+    const uint32_t grp = lane >> 3;        // micro-block within the warp
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < nmicro; j += warps) {
-        const uint32_t g = j * kMicro + lane;
-        const bool in = g < n;
-        const uint64_t c = in ? make_entry(ld_u1(A + g), g, mode) : kEntryNone;
-        uint64_t p = c, s = c;
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w * 4u < nmicro;
+         w += warps) {
+        const uint32_t j = w * 4u + grp;
+        const uint32_t g0 = j * kMicro + sub * 4u;   // may pass n (then nothing is valid)
+        uint32_t b[4];
+        if (aligned && g0 + 3u < n) {
+            const uint4 f = ld_u4(A + g0);
+            b[0] = f.x;
+            b[1] = f.y;
+            b[2] = f.z;
+            b[3] = f.w;
+        } else {
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint64_t tp = __shfl_up_sync(0xffffffffu, p, o);
-            const uint64_t ts = __shfl_down_sync(0xffffffffu, s, o);
-            if (lane >= static_cast<uint32_t>(o) && tp < p) p = tp;
-            if (lane + o < 32u && ts < s) s = ts;
+            for (int k = 0; k < 4; ++k) b[k] = (g0 + k < n) ? ld_u1(A + g0 + k) : 0u;
         }
-        if (in) {
-            st_entry(mpre + g, p);
-            st_entry(msuf + g, s);
-            if (lane == 0) mst0[j] = s;
+        Entry p[4], q[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p[k] = (g0 + k < n) ? make_entry(b[k], g0 + k, mode) : kEntryNone;
+        q[3] = p[3];
+#pragma unroll
+        for (int k = 2; k >= 0; --k) q[k] = better(p[k], q[k + 1]);
+#pragma unroll
+        for (int k = 1; k < 4; ++k) p[k] = better(p[k - 1], p[k]);
+        // lane totals scanned across the 8 lanes of the micro-block
+        Entry ip = p[3], is = q[0];
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const Entry tp = __shfl_up_sync(0xffffffffu, ip, o, 8);
+            const Entry ts = __shfl_down_sync(0xffffffffu, is, o, 8);
+            if (sub >= static_cast<uint32_t>(o)) ip = better(ip, tp);
+            if (sub + o < 8u) is = better(is, ts);
+        }
+        Entry ep = __shfl_up_sync(0xffffffffu, ip, 1, 8);
+        Entry es = __shfl_down_sync(0xffffffffu, is, 1, 8);
+        if (sub == 0u) ep = kEntryNone;
+        if (sub == 7u) es = kEntryNone;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            p[k] = better(ep, p[k]);
+            q[k] = better(es, q[k]);
+        }
+        if (j < nmicro) {
+            if (g0 + 3u < n) {
+                __stcs(reinterpret_cast<ulonglong2 *>(mpre + g0), make_ulonglong2(p[0], p[1]));
+                __stcs(reinterpret_cast<ulonglong2 *>(mpre + g0 + 2), make_ulonglong2(p[2], p[3]));
+                __stcs(reinterpret_cast<ulonglong2 *>(msuf + g0), make_ulonglong2(q[0], q[1]));
+                __stcs(reinterpret_cast<ulonglong2 *>(msuf + g0 + 2), make_ulonglong2(q[2], q[3]));
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (g0 + k < n) {
+                        st_entry(mpre + g0 + k, p[k]);
+                        st_entry(msuf + g0 + k, q[k]);
+                    }
+            }
+            if (sub == 0u) mst0[j] = q[0];
         }
     }
 }
@@ -183,10 +227,11 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     err = launch_levels(p.st, p.nb, p.levels, dev, s);
     if (err != cudaSuccess || !p.micro) return err;
 
-    uint32_t g = (p.nmicro + 7) / 8;  // 8 warps per CTA, one micro-block per warp
+    uint32_t g = (p.nmicro + 31) / 32;  // 8 warps per CTA, 4 micro-blocks per warp
     const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
     if (g > cap) g = cap;
-    micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst, p.kmode);
+    micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst, p.kmode,
+                                        p.aligned);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     return launch_levels(p.mst, p.nmicro, p.mlevels, dev, s);

@@ -231,3 +231,29 @@ def test_power_sampler_against_fake_nvml(native, tmp_path, monkeypatch):
     monkeypatch.setenv("RTXRMQ_NVML_LIBRARY", str(tmp_path / "missing.so"))
     with PowerSampler(0) as q:
         assert not q.available and q.status == -5
+
+
+def test_bench_and_entry_compile():
+    """bench.py and __graft_entry__.py are valid Python (the GPU legs are
+    only exercised on a GPU; this catches syntax errors on the CPU)."""
+    import py_compile
+    root = Path(__file__).resolve().parent.parent
+    for f in ("bench.py", "__graft_entry__.py"):
+        py_compile.compile(str(root / f), doraise=True)
+
+
+def test_bench_reference_arm(native, oracle_lib):
+    """`bench.py --impl reference` (the reference's CPU comparator, HRMQ
+    restated) prints one JSON line with the contract's keys."""
+    import json
+    import subprocess
+    import sys
+    root = Path(__file__).resolve().parent.parent
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n", "1000000",
+                        "--q", "100000", "--steps", "3", "--warmup", "3"],
+                       cwd=root, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads([x for x in r.stdout.splitlines() if x.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "RMQ/s"
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["steps"] == 3
