@@ -232,7 +232,9 @@ int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
  * the queries d_queries[h_qstarts[i] .. h_qstarts[i] + h_qcounts[i]) (int32
  * pairs in array-local coordinates); outputs are written at the queries'
  * positions, indices array-local. Arrays and query ranges may sit anywhere
- * in their buffers (gaps allowed). Arrays are grouped into size buckets
+ * in their buffers (gaps allowed). An array may be empty (length 0): it has
+ * no structure, and every query it owns is invalid (index -1, value NaN,
+ * counted by rmq_batch_invalid_count). Arrays are grouped into size buckets
  * floor(log2 length); h_bucket_bs[bucket] (RMQ_BATCH_BUCKETS entries, or
  * NULL; <= 0 means default) is the block size of that bucket, as chosen by
  * rmq_batch_autotune.

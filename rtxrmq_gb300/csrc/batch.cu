@@ -165,7 +165,7 @@ scatter_grad_kernel(const BatchArray *arrays, const uint4 *qitems, int32_t nqite
     }
 }
 
-int g_batch_per_sm[2] = {0, 0};
+std::atomic<int> g_batch_per_sm[2];
 
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -231,23 +231,24 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
     for (int32_t i = 0; i < narrays; ++i) {
         const int64_t n = h_lengths[i], s = h_starts[i];
         const int64_t qs = h_qstarts[i], qc = h_qcounts[i];
-        if (n <= 0 || n > 0x7fffffffLL || s < 0 || qs < 0 || qc < 0 || qc > 0xffffffffLL) {
+        if (n < 0 || n > 0x7fffffffLL || s < 0 || qs < 0 || qc < 0 || qc > 0xffffffffLL) {
             delete b;
             return set_error(RMQ_EINVAL,
                              "rmq_batch_create: array %d has start=%lld length=%lld qstart=%lld "
-                             "qcount=%lld (need length in [1, 2^31-1], others >= 0)",
+                             "qcount=%lld (need length in [0, 2^31-1], others >= 0)",
                              i, (long long)s, (long long)n, (long long)qs, (long long)qc);
         }
-        int64_t bs = b->bucket_bs[bucket_of(n)];
+        // an empty array has no structure; its queries (if any) are invalid
+        int64_t bs = n > 0 ? b->bucket_bs[bucket_of(n)] : 1;
         if (bs <= 0) bs = default_bs(n);
-        if (bs > n) bs = n;
+        if (bs > n) bs = n > 0 ? n : 1;
         BatchArray &a = b->h_arrays[i];
         a.off = s;
         a.qoff = qs;
         a.n = static_cast<uint32_t>(n);
         a.bs = static_cast<uint32_t>(bs);
         a.nb = static_cast<uint32_t>((n + bs - 1) / bs);
-        a.levels = st_levels(a.nb);
+        a.levels = a.nb > 0 ? st_levels(a.nb) : 0u;
         a.U = make_unit_layout(a.bs, a.nb);
         a.dv = make_div31(a.bs);
         a.pre = ws_entries;
@@ -366,16 +367,12 @@ int rmq_batch_run(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
     const bool aligned = reinterpret_cast<uintptr_t>(d_vals) % 16 == 0;
     void *kern = aligned ? reinterpret_cast<void *>(batch_kernel<true>)
                          : reinterpret_cast<void *>(batch_kernel<false>);
-    int &per_sm = g_batch_per_sm[aligned ? 1 : 0];
-    cudaError_t err = cudaSuccess;
-    if (per_sm == 0) {
-        err = aligned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<true>,
-                                                                      kThreads, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<false>,
-                                                                      kThreads, 0);
-        if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run: occupancy");
-        if (per_sm < 1) return set_error(RMQ_ENOTSUP, "rmq_batch_run: kernel cannot be resident");
-    }
+    int per_sm;
+    cudaError_t err = aligned ? occupancy_cached(batch_kernel<true>, kThreads, g_batch_per_sm[1], per_sm)
+                              : occupancy_cached(batch_kernel<false>, kThreads, g_batch_per_sm[0], per_sm);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run: occupancy");
+    // a cooperative launch needs every CTA resident
+    if (per_sm < 1) return set_error(RMQ_ENOTSUP, "rmq_batch_run: kernel cannot be resident");
     const unsigned grid = static_cast<unsigned>(dev.sms * per_sm);
     void *args[] = {&P};
     err = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, stream);
@@ -489,8 +486,8 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts, const int64_t *
     if (reps < 1) reps = 1;
     std::vector<std::vector<int32_t>> members(RMQ_BATCH_BUCKETS);
     for (int32_t i = 0; i < narrays; ++i) {
-        if (h_lengths[i] <= 0) return set_error(RMQ_EINVAL, "rmq_batch_autotune: empty array %d", i);
-        members[bucket_of(h_lengths[i])].push_back(i);
+        if (h_lengths[i] < 0) return set_error(RMQ_EINVAL, "rmq_batch_autotune: array %d length < 0", i);
+        if (h_lengths[i] > 0) members[bucket_of(h_lengths[i])].push_back(i);  // empty: no structure
     }
     static const int32_t cands[] = {64, 256, 1024, 4096, 16384, 65536};
     cudaEvent_t e0, e1;

@@ -120,7 +120,7 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
     }
 }
 
-int g_units_per_sm[2] = {0, 0};
+std::atomic<int> g_units_per_sm[2];
 
 cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceInfo &dev,
                           cudaStream_t s) {
@@ -204,18 +204,16 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     J.kmode = p.kmode;
     const uint32_t nunits = unit_count(p.nb, J.U);
 
-    cudaError_t err;
-    int &per_sm = g_units_per_sm[p.aligned ? 1 : 0];
-    if (per_sm == 0) {
-        // every key mode compiles to the same resources; the float-min
-        // instantiation stands for all four
-        err = p.aligned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, build_units_kernel<true, kFloatMin>, kBuildThreads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, build_units_kernel<false, kFloatMin>, kBuildThreads, 0);
-        if (err != cudaSuccess) return err;
-        if (per_sm < 1) per_sm = 1;
-    }
+    // every key mode compiles to the same resources; the float-min
+    // instantiation stands for all four
+    int per_sm;
+    cudaError_t err =
+        p.aligned ? occupancy_cached(build_units_kernel<true, kFloatMin>, kBuildThreads,
+                                     g_units_per_sm[1], per_sm)
+                  : occupancy_cached(build_units_kernel<false, kFloatMin>, kBuildThreads,
+                                     g_units_per_sm[0], per_sm);
+    if (err != cudaSuccess) return err;
+    if (per_sm < 1) per_sm = 1;
     uint32_t grid = static_cast<uint32_t>(dev.sms) * static_cast<uint32_t>(per_sm);
     if (grid > nunits) grid = nunits;
     if (p.aligned)

@@ -2,6 +2,7 @@
 // translation units. Nothing here is exported.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -22,6 +23,21 @@ struct DeviceInfo {
     size_t l2_bytes;
 };
 int device_info(DeviceInfo *out);
+
+// Resident CTAs per SM of `kernel` at `threads` threads (no dynamic shared
+// memory), computed once per cache slot; concurrent first callers compute
+// and store the same value.
+template <class K>
+cudaError_t occupancy_cached(K kernel, int threads, std::atomic<int> &cache, int &per_sm) {
+    int v = cache.load(std::memory_order_relaxed);
+    if (v == 0) {
+        const cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0);
+        if (err != cudaSuccess) return err;
+        cache.store(v, std::memory_order_relaxed);
+    }
+    per_sm = v;
+    return cudaSuccess;
+}
 
 // ---- plain index (build.cu) ----
 struct BuildPlan {

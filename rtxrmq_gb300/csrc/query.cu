@@ -95,18 +95,15 @@ scan_kernel(const float *__restrict__ A, uint32_t n, QueryOut o, int64_t q) {
     }
 }
 
-int g_query_per_sm[2] = {0, 0};
-int g_gather_per_sm = 0;
-int g_scan_per_sm = 0;
+std::atomic<int> g_query_per_sm[2];
+std::atomic<int> g_gather_per_sm{0};
+std::atomic<int> g_scan_per_sm{0};
 
 template <typename K>
-cudaError_t occupancy(K kernel, int *cache) {
-    if (*cache) return cudaSuccess;
-    int per_sm = 0;
-    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
-    if (err != cudaSuccess) return err;
-    *cache = per_sm < 1 ? 1 : per_sm;
-    return cudaSuccess;
+cudaError_t occupancy(K kernel, std::atomic<int> *cache, int *per_sm) {
+    const cudaError_t err = occupancy_cached(kernel, kThreads, *cache, *per_sm);
+    if (*per_sm < 1) *per_sm = 1;
+    return err;
 }
 
 uint32_t grid_size(int64_t q, int64_t per_block, int per_sm, const DeviceInfo &dev) {
@@ -148,15 +145,17 @@ cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInf
     o.invalid = a.invalid;
     cudaError_t err;
     if (p.aligned) {
-        err = occupancy(query_kernel<true>, &g_query_per_sm[1]);
+        int per_sm;
+        err = occupancy(query_kernel<true>, &g_query_per_sm[1], &per_sm);
         if (err != cudaSuccess) return err;
-        query_kernel<true><<<grid_size(a.q, kThreads * kQPT, g_query_per_sm[1], dev), kThreads, 0,
-                             s>>>(v, o, a.q);
+        query_kernel<true><<<grid_size(a.q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(
+            v, o, a.q);
     } else {
-        err = occupancy(query_kernel<false>, &g_query_per_sm[0]);
+        int per_sm;
+        err = occupancy(query_kernel<false>, &g_query_per_sm[0], &per_sm);
         if (err != cudaSuccess) return err;
-        query_kernel<false><<<grid_size(a.q, kThreads * kQPT, g_query_per_sm[0], dev), kThreads,
-                              0, s>>>(v, o, a.q);
+        query_kernel<false><<<grid_size(a.q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(
+            v, o, a.q);
     }
     return cudaGetLastError();
 }
@@ -170,24 +169,25 @@ cudaError_t launch_probe_gather(const BuildPlan &p, const QueryArgs &a, const De
     o.val = a.val;
     o.idx = a.idx;
     o.invalid = nullptr;
-    cudaError_t err = occupancy(gather_kernel, &g_gather_per_sm);
+    int per_sm;
+    cudaError_t err = occupancy(gather_kernel, &g_gather_per_sm, &per_sm);
     if (err != cudaSuccess) return err;
-    gather_kernel<<<grid_size(a.q, kThreads * kQPT, g_gather_per_sm, dev), kThreads, 0, s>>>(v, o,
-                                                                                            a.q);
+    gather_kernel<<<grid_size(a.q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(v, o, a.q);
     return cudaGetLastError();
 }
 
 cudaError_t launch_query_scan(const float *A, uint32_t n, const QueryArgs &a,
                               const DeviceInfo &dev, cudaStream_t s) {
     if (a.q <= 0) return cudaSuccess;
-    cudaError_t err = occupancy(scan_kernel, &g_scan_per_sm);
+    int per_sm;
+    cudaError_t err = occupancy(scan_kernel, &g_scan_per_sm, &per_sm);
     if (err != cudaSuccess) return err;
     QueryOut o;
     o.Q = a.Q;
     o.val = a.val;
     o.idx = a.idx;
     o.invalid = a.invalid;
-    scan_kernel<<<grid_size(a.q, kThreads, g_scan_per_sm, dev), kThreads, 0, s>>>(A, n, o, a.q);
+    scan_kernel<<<grid_size(a.q, kThreads, per_sm, dev), kThreads, 0, s>>>(A, n, o, a.q);
     return cudaGetLastError();
 }
 

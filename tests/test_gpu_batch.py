@@ -110,6 +110,41 @@ def test_batch_invalid_and_repeat(cuda, native, oracle_lib):
         assert b.invalid_count() == 12
 
 
+def test_batch_empty_arrays_and_no_queries(cuda, native, oracle_lib):
+    """Empty arrays (length 0) are allowed: no structure, their queries are
+    invalid; q = 0 runs are no-ops on every entry point; the per-array path
+    and the autotuner accept the same plan."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    from rtxrmq_gb300.batch import RMQBatch, autotune
+    starts = np.array([0, 64, 64, 300], np.int64)
+    lengths = np.array([64, 0, 236, 0], np.int64)
+    qstarts = np.array([0, 2, 4, 6], np.int64)
+    qcounts = np.array([2, 2, 2, 0], np.int64)
+    Q = np.array([[0, 63], [10, 20], [0, 0], [0, 5], [0, 235], [100, 200]], np.int32)
+    A = R.gen_values_uniform(300, 3)
+    dA, dQ = torch.from_numpy(A).to(cuda), torch.from_numpy(Q).to(cuda)
+    want = [int(np.argmin(A[:64])), 10 + int(np.argmin(A[10:21])), -1, -1,
+            int(np.argmin(A[64:300])), 100 + int(np.argmin(A[164:265]))]
+    for cfg in (None, autotune(starts, lengths, qstarts, qcounts, dA, dQ, reps=1, cache=None)):
+        with RMQBatch(starts, lengths, qstarts, qcounts, cfg) as b:
+            v, i = b.run(dA, dQ)
+            assert list(i.cpu().numpy()) == want
+            v2, i2 = b.run_per_array(dA, dQ)
+            assert list(i2.cpu().numpy()) == want
+            assert b.invalid_count() == 4
+    # q = 0 on the plain entry points
+    with R.RMQIndex(dA, 64) as ix:
+        empty = torch.empty((0, 2), dtype=torch.int32, device=cuda)
+        v, i = ix.query(empty)
+        assert v.numel() == 0 and i.numel() == 0
+        ix.query_host(np.empty((0, 2), np.int32), np.empty(0, np.float32), np.empty(0, np.int32))
+        ix.probe_gather(empty)
+        torch.cuda.synchronize()
+        assert ix.invalid_count() == 0
+
+
 def test_batch_graph_capture(cuda, native, oracle_lib):
     """rmq_batch_run captured once in a CUDA graph and replayed on new data."""
     import torch
