@@ -55,8 +55,8 @@ int set_error(int code, const char *fmt, ...) {
 }
 
 int cuda_fail(cudaError_t err, const char *what) {
-    return set_error(RMQ_ECUDA, "%s: %s (%s)", what, cudaGetErrorName(err),
-                     cudaGetErrorString(err));
+    return set_error(err == cudaErrorMemoryAllocation ? RMQ_ENOMEM : RMQ_ECUDA, "%s: %s (%s)",
+                     what, cudaGetErrorName(err), cudaGetErrorString(err));
 }
 
 int device_info(DeviceInfo *out) {
@@ -152,6 +152,7 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
 
 int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq_stream_t stream,
                  rmq_handle_t **out) {
+    NvtxRange nvtx_range("rmq_build_ex");
     g_err[0] = '\0';
     if (!out) return set_error(RMQ_EINVAL, "rmq_build: out is NULL");
     if (flags & ~static_cast<uint32_t>(RMQ_BUILD_NO_MICRO | RMQ_BUILD_MAX | RMQ_BUILD_INT32))
@@ -186,7 +187,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
         return set_error(RMQ_ENOMEM, "rmq_build: host allocation failed");
     }
     h->device = dev.device;
-    cudaError_t err = cudaMalloc(&h->mem, total);
+    cudaError_t err = dev_malloc(&h->mem, total);
     if (err != cudaSuccess) {
         delete h->host_mu;
         delete h;
@@ -214,6 +215,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
 
 int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float *d_val,
               int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_query");
     g_err[0] = '\0';
     if (!h) return set_error(RMQ_EINVAL, "rmq_query: handle is NULL");
     if (q < 0) return set_error(RMQ_EINVAL, "rmq_query: q=%lld < 0", (long long)q);
@@ -244,6 +246,7 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float 
 
 int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float *d_val,
                      int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_probe_gather");
     g_err[0] = '\0';
     if (!h) return set_error(RMQ_EINVAL, "rmq_probe_gather: handle is NULL");
     if (q < 0) return set_error(RMQ_EINVAL, "rmq_probe_gather: q=%lld < 0", (long long)q);
@@ -269,6 +272,36 @@ int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
     cudaError_t err = launch_probe_gather(h->plan, a, dev, stream);
     if (err != cudaSuccess) return cuda_fail(err, "rmq_probe_gather: launch");
     return RMQ_OK;
+}
+
+// Streams, events and buffer of the rmq_query_host pipeline, whatever part
+// of them exists (after waiting for their work); the handle then has none.
+static cudaError_t release_staging(rmq_handle_t *h) {
+    cudaStream_t *streams[] = {&h->hs, &h->ks, &h->cs};
+    for (cudaStream_t *st : streams)
+        if (*st) {
+            cudaStreamSynchronize(*st);
+            cudaStreamDestroy(*st);
+            *st = nullptr;
+        }
+    for (int s = 0; s < kHostStreams; ++s) {
+        cudaEvent_t *evs[] = {&h->h_done[s], &h->k_done[s], &h->c_done[s]};
+        for (cudaEvent_t *e : evs)
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
+    }
+    cudaEvent_t *evs[] = {&h->ev_start, &h->ev_end};
+    for (cudaEvent_t *e : evs)
+        if (*e) {
+            cudaEventDestroy(*e);
+            *e = nullptr;
+        }
+    cudaError_t err = cudaSuccess;
+    if (h->stage) err = cudaFree(h->stage);
+    h->stage = nullptr;
+    return err;
 }
 
 // True when p is device (or managed) memory of the current context.
@@ -303,6 +336,7 @@ static const void *device_address(const void *p) {
 
 int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, float *h_val,
                    int32_t *h_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_query_host");
     g_err[0] = '\0';
     if (!h) return set_error(RMQ_EINVAL, "rmq_query_host: handle is NULL");
     if (q < 0) return set_error(RMQ_EINVAL, "rmq_query_host: q=%lld < 0", (long long)q);
@@ -343,8 +377,9 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
     std::lock_guard<std::mutex> lock(*hm->host_mu);
     cudaError_t err = cudaSuccess;
     if (!hm->stage) {
-        err = cudaMalloc(&hm->stage, kHostStreams * kHostChunk * 16);
-        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->hs, cudaStreamNonBlocking);
+        // streams and events first, the staging buffer last: `stage` set
+        // means the whole pipeline exists; a failure leaves none of it
+        err = cudaStreamCreateWithFlags(&hm->hs, cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->ks, cudaStreamNonBlocking);
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&hm->cs, cudaStreamNonBlocking);
         for (int s = 0; s < kHostStreams && err == cudaSuccess; ++s) {
@@ -354,7 +389,11 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
         }
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->ev_start, cudaEventDisableTiming);
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&hm->ev_end, cudaEventDisableTiming);
-        if (err != cudaSuccess) return cuda_fail(err, "rmq_query_host: staging set-up");
+        if (err == cudaSuccess) err = dev_malloc(&hm->stage, kHostStreams * kHostChunk * 16);
+        if (err != cudaSuccess) {
+            release_staging(hm);
+            return cuda_fail(err, "rmq_query_host: staging set-up");
+        }
     }
     err = cudaEventRecord(hm->ev_start, stream);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(hm->hs, hm->ev_start, 0);
@@ -416,29 +455,7 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
 int rmq_free(rmq_handle_t *h) {
     g_err[0] = '\0';
     if (!h) return RMQ_OK;
-    cudaError_t err = cudaSuccess;
-    if (h->stage) {
-        if (h->hs) {
-            cudaStreamSynchronize(h->hs);
-            cudaStreamDestroy(h->hs);
-        }
-        if (h->ks) {
-            cudaStreamSynchronize(h->ks);
-            cudaStreamDestroy(h->ks);
-        }
-        if (h->cs) {
-            cudaStreamSynchronize(h->cs);
-            cudaStreamDestroy(h->cs);
-        }
-        for (int s = 0; s < kHostStreams; ++s) {
-            if (h->h_done[s]) cudaEventDestroy(h->h_done[s]);
-            if (h->k_done[s]) cudaEventDestroy(h->k_done[s]);
-            if (h->c_done[s]) cudaEventDestroy(h->c_done[s]);
-        }
-        if (h->ev_start) cudaEventDestroy(h->ev_start);
-        if (h->ev_end) cudaEventDestroy(h->ev_end);
-        err = cudaFree(h->stage);
-    }
+    cudaError_t err = release_staging(h);
     cudaError_t e2 = cudaFree(h->mem);
     if (err == cudaSuccess) err = e2;
     delete h->host_mu;
@@ -479,6 +496,7 @@ int rmq_invalid_count(const rmq_handle_t *h, rmq_stream_t stream, int64_t *count
 
 int rmq_query_scan(const float *d_vals, int64_t n, const int32_t *d_queries, int64_t q,
                    float *d_val, int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_query_scan");
     g_err[0] = '\0';
     if (n <= 0 || n > 0x7fffffffLL)
         return set_error(RMQ_EINVAL, "rmq_query_scan: n=%lld outside [1, 2^31-1]", (long long)n);

@@ -205,6 +205,7 @@ extern "C" {
 int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
                      const int64_t *h_qstarts, const int64_t *h_qcounts,
                      const int32_t *h_bucket_bs, rmq_batch_t **out) {
+    NvtxRange nvtx_range("rmq_batch_create");
     if (!out) return set_error(RMQ_EINVAL, "rmq_batch_create: out is NULL");
     *out = nullptr;
     if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts)
@@ -297,7 +298,7 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
     const size_t o_ws = align_up(o_cnt + 256, 256);
     b->ws_bytes = sizeof(Entry) * static_cast<size_t>(ws_entries);
     b->mem_bytes = o_ws + b->ws_bytes;
-    cudaError_t err = cudaMalloc(&b->mem, b->mem_bytes);
+    cudaError_t err = dev_malloc(&b->mem, b->mem_bytes);
     if (err != cudaSuccess) {
         cudaGetLastError();
         size_t bytes = b->mem_bytes;
@@ -354,6 +355,7 @@ static int batch_args(const rmq_batch_t *b, const float *d_vals, const int32_t *
 
 int rmq_batch_run(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries, float *d_val,
                   int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_batch_run");
     int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_run");
     if (rc) return rc;
     DeviceInfo dev;
@@ -382,6 +384,7 @@ int rmq_batch_run(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
 
 int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
                             float *d_val, int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_batch_run_per_array");
     int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_run_per_array");
     if (rc) return rc;
     DeviceInfo dev;
@@ -426,6 +429,7 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
 
 int rmq_batch_scatter_grad(const rmq_batch_t *b, const int32_t *d_idx, const float *d_grad_out,
                            float *d_grad_vals, int32_t accumulate, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_batch_scatter_grad");
     if (!b || !d_idx || !d_grad_out || !d_grad_vals)
         return set_error(RMQ_EINVAL, "rmq_batch_scatter_grad: NULL argument");
     DeviceInfo dev;
@@ -481,6 +485,7 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts, const int64_t *
                        const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
                        const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
                        rmq_stream_t stream, int32_t *h_bucket_bs) {
+    NvtxRange nvtx_range("rmq_batch_autotune");
     if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts || !h_bucket_bs)
         return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
     if (reps < 1) reps = 1;

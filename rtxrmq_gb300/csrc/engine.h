@@ -4,8 +4,11 @@
 
 #include <atomic>
 #include <cstddef>
+#include <cstdlib>
 #include <cstdint>
 #include <cuda_runtime.h>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "common.cuh"
 
@@ -23,6 +26,27 @@ struct DeviceInfo {
     size_t l2_bytes;
 };
 int device_info(DeviceInfo *out);
+
+// NVTX range over one C-ABI call (named after it), visible to profilers
+// and tracers; nearly free when none is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
+// Every device allocation of the library goes through here. Fault
+// injection for tests: with RTXRMQ_FAIL_ALLOC=1 in the environment it
+// fails as an out-of-memory would, without touching the device.
+inline cudaError_t dev_malloc(void **p, size_t bytes) {
+    const char *f = std::getenv("RTXRMQ_FAIL_ALLOC");
+    if (f && f[0] == '1') {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
 
 // Resident CTAs per SM of `kernel` at `threads` threads (no dynamic shared
 // memory), computed once per cache slot; concurrent first callers compute

@@ -61,6 +61,7 @@ using namespace rmq;
 extern "C" int rmq_query_noalloc(const float *d_vals, int64_t n, int64_t bs,
                                  const int32_t *d_queries, int64_t q, float *d_val,
                                  int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_query_noalloc");
     if (n <= 0 || n > 0x7fffffffLL)
         return set_error(RMQ_EINVAL, "rmq_query_noalloc: n=%lld outside [1, 2^31-1]", (long long)n);
     if (!d_vals || reinterpret_cast<uintptr_t>(d_vals) % 4)

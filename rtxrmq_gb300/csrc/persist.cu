@@ -68,7 +68,7 @@ __global__ void fingerprint_kernel(const float *__restrict__ A, uint32_t n,
 
 int fingerprint(const float *A, uint32_t n, cudaStream_t s, uint64_t *out) {
     unsigned long long *d = nullptr;
-    cudaError_t err = cudaMalloc(&d, sizeof(*d));
+    cudaError_t err = dev_malloc(reinterpret_cast<void **>(&d), sizeof(*d));
     if (err != cudaSuccess) return cuda_fail(err, "fingerprint: cudaMalloc");
     DeviceInfo dev;
     int rc = device_info(&dev);
@@ -105,6 +105,7 @@ using namespace rmq;
 extern "C" {
 
 int rmq_save(const rmq_handle_t *h, const char *path, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_save");
     if (!h || !path) return set_error(RMQ_EINVAL, "rmq_save: NULL argument");
     BuildPlan p;
     void *mem = nullptr;
@@ -155,6 +156,7 @@ int rmq_save(const rmq_handle_t *h, const char *path, rmq_stream_t stream) {
 
 int rmq_load(const float *d_vals, int64_t n, const char *path, rmq_stream_t stream,
              rmq_handle_t **out) {
+    NvtxRange nvtx_range("rmq_load");
     if (!out || !path || !d_vals) return set_error(RMQ_EINVAL, "rmq_load: NULL argument");
     *out = nullptr;
     if (n <= 0 || n > 0x7fffffffLL) return set_error(RMQ_EINVAL, "rmq_load: bad n=%lld", (long long)n);
@@ -198,7 +200,7 @@ int rmq_load(const float *d_vals, int64_t n, const char *path, rmq_stream_t stre
                          "rmq_load: the values differ from those the index was built from");
     }
     void *mem = nullptr;
-    cudaError_t err = cudaMalloc(&mem, bytes);
+    cudaError_t err = dev_malloc(&mem, bytes);
     if (err != cudaSuccess) {
         std::fclose(fp);
         cudaGetLastError();

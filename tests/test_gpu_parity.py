@@ -432,3 +432,45 @@ def test_probe_gather(cuda, native, oracle_lib):
     assert_matches(A, Q, v.cpu().numpy(), i.cpu().numpy(), ev, ei)
     ib = ib.cpu().numpy()
     assert ((ib >= 0) & (ib < n)).all()
+
+
+def test_allocation_failure_injection(cuda, native, oracle_lib, monkeypatch, tmp_path):
+    """Host-side fault injection (RTXRMQ_FAIL_ALLOC=1 makes every device
+    allocation of the library fail as out-of-memory): each allocating call
+    returns RMQ_ENOMEM with a message, nothing leaks or breaks, and the same
+    calls succeed once the variable is cleared. No GPU fault is involved."""
+    import torch
+
+    import oracle
+    import rtxrmq_gb300 as R
+    from rtxrmq_gb300._native import RMQ_ENOMEM
+    from rtxrmq_gb300.batch import RMQBatch
+    rng = np.random.default_rng(3)
+    A = rng.random(20000).astype(np.float32)
+    Q = R.gen_queries(5000, len(A), -3, 4)
+    dA = torch.from_numpy(A).to(cuda)
+    ei = oracle.base_idx(A, Q)
+    with R.RMQIndex(dA, 1024) as ix:
+        ix.save(tmp_path / "ix.rmq")
+        monkeypatch.setenv("RTXRMQ_FAIL_ALLOC", "1")
+        with pytest.raises(R.RMQError) as e:
+            R.RMQIndex(dA, 1024)
+        assert e.value.code == RMQ_ENOMEM and "failed" in str(e.value)
+        with pytest.raises(R.RMQError):
+            RMQBatch([0], [len(A)], [0], [len(Q)])
+        with pytest.raises(R.RMQError):
+            R.RMQIndex.load(dA, tmp_path / "ix.rmq")
+        monkeypatch.setenv("RTXRMQ_HOST_STAGED", "1")  # needs its staging allocation
+        hv, hi = np.empty(len(Q), np.float32), np.empty(len(Q), np.int32)
+        with pytest.raises(R.RMQError):
+            ix.query_host(Q, hv, hi)
+        # the existing index is untouched and answers on the device
+        v, i = ix.query(torch.from_numpy(Q).to(cuda))
+        np.testing.assert_array_equal(i.cpu().numpy(), ei)
+        monkeypatch.delenv("RTXRMQ_FAIL_ALLOC")
+        ix.query_host(Q, hv, hi)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(hi, ei)
+    with R.RMQIndex.load(dA, tmp_path / "ix.rmq") as ix2:
+        v, i = ix2.query(torch.from_numpy(Q).to(cuda))
+        np.testing.assert_array_equal(i.cpu().numpy(), ei)
