@@ -220,6 +220,14 @@ int rmq_query_scan(const float *d_vals, int64_t n, const int32_t *d_queries,
 int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
                      float *d_val, int32_t *d_idx, rmq_stream_t stream);
 
+/*
+ * Checked builds only, no reference counterpart (the library compiled with
+ * -DRMQ_CHECKED=1, a stand-in for a memory sanitizer): the number of
+ * out-of-range global accesses the kernels caught and skipped since the
+ * library was loaded. RMQ_ENOTSUP (count 0) in normal builds.
+ */
+int rmq_checked_violations(int64_t *count);
+
 /* ------------------------------------------------------------------------
  * Batched ragged form: many independent arrays of uneven length, each with
  * its own queries, built and answered by ONE persistent cooperative kernel

@@ -70,6 +70,7 @@ SIGNATURES = {
     "rmq_bs_from_nb": (C.c_int, [_i64, _i64, C.POINTER(_i64)]),
     "rmq_query_scan": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_probe_gather": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "rmq_checked_violations": (C.c_int, [C.POINTER(_i64)]),
     "rmq_batch_create": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
     "rmq_batch_run": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_run_per_array": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),

@@ -61,12 +61,18 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build failed:\n  " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile librmq.so and the rtxrmq CLI; return the library path."""
+def build(verbose: bool = False, force: bool = False, checked: bool = False) -> Path:
+    """Compile librmq.so and the rtxrmq CLI; return the library path.
+
+    checked=True builds the range-checked variant (-DRMQ_CHECKED=1: every
+    global index the kernels use is checked, violations are counted and
+    skipped, read back with rmq_checked_violations) into _lib/checked/."""
     nvcc = _nvcc()
     cuda = _cuda_home(nvcc)
-    OUT.mkdir(exist_ok=True)
-    obj_dir = OUT / "obj"
+    out_dir = OUT / "checked" if checked else OUT
+    flags = NVCC_FLAGS + (["-DRMQ_CHECKED=1"] if checked else [])
+    out_dir.mkdir(parents=True, exist_ok=True)
+    obj_dir = out_dir / "obj"
     obj_dir.mkdir(exist_ok=True)
     hdrs = _headers()
     inc = [f"-I{INCLUDE}", f"-I{CSRC}", f"-I{cuda / 'include'}"]
@@ -75,7 +81,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     for src in LIB_CU:
         o = obj_dir / (src + ".o")
         if force or _stale(o, [CSRC / src, *hdrs]):
-            jobs.append([nvcc, *NVCC_FLAGS, *inc, "-c", str(CSRC / src), "-o", str(o)])
+            jobs.append([nvcc, *flags, *inc, "-c", str(CSRC / src), "-o", str(o)])
     for src in LIB_CPP + CLI_CPP:
         o = obj_dir / (src + ".o")
         if force or _stale(o, [CSRC / src, *hdrs]):
@@ -86,15 +92,15 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(_run, jobs))
 
-    lib = OUT / "librmq.so"
+    lib = out_dir / "librmq.so"
     lib_objs = [obj_dir / (s + ".o") for s in LIB_CU + LIB_CPP]
     if force or _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs),
               "-Xcompiler", "-fopenmp", "-lgomp", "-ldl", "-lpthread"])
-    cli = OUT / "rtxrmq"
+    cli = out_dir / "rtxrmq"
     cli_objs = [obj_dir / (s + ".o") for s in CLI_CPP]
     if force or _stale(cli, cli_objs + [lib]):
-        _run(["g++", "-o", str(cli), *map(str, cli_objs), f"-L{OUT}", "-lrmq",
+        _run(["g++", "-o", str(cli), *map(str, cli_objs), f"-L{out_dir}", "-lrmq",
               "-Wl,-rpath,$ORIGIN", f"-L{cuda / 'lib64'}", "-lcudart", "-fopenmp"])
     return lib
 

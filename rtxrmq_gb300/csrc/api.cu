@@ -494,6 +494,21 @@ int rmq_invalid_count(const rmq_handle_t *h, rmq_stream_t stream, int64_t *count
     return RMQ_OK;
 }
 
+int rmq_checked_violations(int64_t *count) {
+    g_err[0] = '\0';
+    if (!count) return set_error(RMQ_EINVAL, "rmq_checked_violations: count is NULL");
+    *count = 0;
+    if (!RMQ_CHECKED)
+        return set_error(RMQ_ENOTSUP, "rmq_checked_violations: not a checked build (RMQ_CHECKED=1)");
+    const unsigned long long parts[] = {violations_build(), violations_query(), violations_batch(),
+                                        violations_persist()};
+    for (unsigned long long v : parts) {
+        if (v == ~0ull) return set_error(RMQ_ECUDA, "rmq_checked_violations: counter read failed");
+        *count += static_cast<int64_t>(v);
+    }
+    return RMQ_OK;
+}
+
 int rmq_query_scan(const float *d_vals, int64_t n, const int32_t *d_queries, int64_t q,
                    float *d_val, int32_t *d_idx, rmq_stream_t stream) {
     NvtxRange nvtx_range("rmq_query_scan");

@@ -70,6 +70,7 @@ struct BatchParams {
     int32_t lvl_start[kMaxLevels + 1];
     const uint4 *qitems;
     int32_t nqitems;
+    int64_t total_q;  // one past the last query any array owns
 };
 
 __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchArray &a) {
@@ -89,6 +90,8 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     v.mpre = nullptr;
     v.msuf = nullptr;
     v.kmode = kFloatMin;
+    v.levels = a.levels;
+    v.mlevels = 0u;
     return v;
 }
 
@@ -106,6 +109,7 @@ __device__ __forceinline__ UnitJob unit_job(const BatchParams &P, uint32_t array
     J.suf = P.ws + a.pre + a.n;
     J.bmin = P.ws + a.st;
     J.kmode = kFloatMin;
+    J.nb = a.nb;
     return J;
 }
 
@@ -131,7 +135,7 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
             Entry *cur = P.ws + a.st + static_cast<int64_t>(k) * a.nb;
             const uint32_t half = 1u << (k - 1);
             for (uint32_t j = w.z + threadIdx.x; j < w.z + w.w; j += kThreads)
-                cur[j] = better(prev[j], prev[j + half]);
+                if (rmq_chk(j + half < a.nb)) cur[j] = better(prev[j], prev[j + half]);
         }
         grid.sync();
     }
@@ -146,6 +150,7 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
         o.val = P.val ? P.val + a.qoff : nullptr;
         o.idx = P.idx ? P.idx + a.qoff : nullptr;
         o.invalid = P.invalid;
+        o.span = P.total_q - a.qoff;
         answer_range<ALIGNED, kQPT>(v, o, w.y, static_cast<int64_t>(w.y) + w.z);
     }
 }
@@ -158,9 +163,11 @@ scatter_grad_kernel(const BatchArray *arrays, const uint4 *qitems, int32_t nqite
         const uint4 w = qitems[it];
         const int64_t qoff = arrays[w.x].qoff + w.y;
         const int64_t off = arrays[w.x].off;
+        const uint32_t n = arrays[w.x].n;
         for (uint32_t j = threadIdx.x; j < w.z; j += kThreads) {
+            // argmins outside the array (-1 for invalid queries) add nothing
             const int32_t li = idx[qoff + j];
-            if (li >= 0) atomicAdd(gvals + off + li, gout[qoff + j]);
+            if (li >= 0 && static_cast<uint32_t>(li) < n) atomicAdd(gvals + off + li, gout[qoff + j]);
         }
     }
 }
@@ -171,6 +178,8 @@ std::atomic<int> g_batch_per_sm[2];
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace
+RMQ_VIOLATIONS_READER(violations_batch)
+
 }  // namespace rmq
 
 using namespace rmq;
@@ -288,6 +297,7 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
     for (int k = maxlev; k < kMaxLevels; ++k) P.lvl_start[k] = P.lvl_start[kMaxLevels];
     P.nbuild = static_cast<int32_t>(build.size());
     P.nqitems = static_cast<int32_t>(b->h_qitems.size());
+    P.total_q = b->total_q;
 
     // one allocation: arrays | build | lvl | qitems | counter | workspace
     const size_t o_arr = 0;

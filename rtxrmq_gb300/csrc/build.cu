@@ -44,7 +44,7 @@ __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
     const uint32_t cnt = nb - (1u << k) + 1;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt;
          j += gridDim.x * blockDim.x)
-        cur[j] = better(prev[j], prev[j + half]);
+        if (rmq_chk(j + half < nb)) cur[j] = better(prev[j], prev[j + half]);
 }
 
 // Sub-block level: 8 lanes per 32-element micro-block, 4 consecutive
@@ -202,6 +202,7 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     J.suf = p.suf;
     J.bmin = p.st;
     J.kmode = p.kmode;
+    J.nb = p.nb;
     const uint32_t nunits = unit_count(p.nb, J.U);
 
     // every key mode compiles to the same resources; the float-min
@@ -234,5 +235,7 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     if (err != cudaSuccess) return err;
     return launch_levels(p.mst, p.nmicro, p.mlevels, dev, s);
 }
+
+RMQ_VIOLATIONS_READER(violations_build)
 
 }  // namespace rmq

@@ -89,6 +89,7 @@ struct UnitJob {
     Entry *suf;   // [n]
     Entry *bmin;  // [nb]
     uint32_t kmode;  // KeyMode (common.cuh)
+    uint32_t nb;     // blocks of the array
 };
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return b < a ? b : a; }
@@ -123,6 +124,15 @@ __device__ __forceinline__ Entry unit_decode(uint64_t c, uint32_t ustart, const 
 __device__ __forceinline__ void st_entry(Entry *p, Entry e) {
     __stcs(reinterpret_cast<uint2 *>(p),
            make_uint2(static_cast<uint32_t>(e), static_cast<uint32_t>(e >> 32)));
+}
+
+// Range-checked stores of the builders (rmq_chk, common.cuh): entry i of a
+// per-element array of the job (pre / suf), block minimum b.
+__device__ __forceinline__ void st_elem(const UnitJob &J, Entry *t, uint32_t i, Entry e) {
+    if (rmq_chk(i < J.n)) st_entry(t + i, e);
+}
+__device__ __forceinline__ void st_bmin(const UnitJob &J, uint32_t b, Entry e) {
+    if (rmq_chk(b < J.nb)) J.bmin[b] = e;
 }
 
 // Exclusive min-scan of one value per thread across the CTA, in thread order
@@ -246,7 +256,7 @@ __device__ __forceinline__ void build_unit_tiles(const UnitJob &J, uint32_t u, E
                 if (g >= a_lo && g < a_hi) {
                     const Entry en = stage[e + e / kBuildEPT];
                     const uint32_t local = static_cast<uint32_t>(g - J.off);
-                    st_entry(out + local, en);
+                    st_elem(J, out, local, en);
                     if (!suffix) {
                         // block minimum = prefix minimum at the block's last element
                         const uint32_t ul = local - ustart;
@@ -256,7 +266,7 @@ __device__ __forceinline__ void build_unit_tiles(const UnitJob &J, uint32_t u, E
                             seg = div31(ul, J.dv);
                             last = last || (ul + 1 == (seg + 1) * J.bs);
                         }
-                        if (last) J.bmin[u * U.G + seg] = en;
+                        if (last) st_bmin(J, u * U.G + seg, en);
                     }
                 }
             }
@@ -382,7 +392,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         const uint32_t e = threadIdx.x + k * kBuildThreads;
         const uint32_t ul = e - static_cast<uint32_t>(lead);
         if (ul < ulen) {
-            st_entry(J.pre + ustart + ul, stage[e + e / kBuildEPT]);
+            st_elem(J, J.pre, ustart + ul, stage[e + e / kBuildEPT]);
         }
     }
     {
@@ -391,7 +401,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         for (uint32_t b = threadIdx.x; b < nblk; b += kBuildThreads) {
             const uint32_t last = min((b + 1u) * J.bs, ulen) - 1u;
             const uint32_t e = last + static_cast<uint32_t>(lead);
-            J.bmin[u * G + b] = stage[e + e / kBuildEPT];
+            st_bmin(J, u * G + b, stage[e + e / kBuildEPT]);
         }
     }
     __syncthreads();
@@ -415,7 +425,7 @@ __device__ __forceinline__ void build_unit_tile(const UnitJob &J, uint32_t u, En
         const uint32_t e = threadIdx.x + k * kBuildThreads;
         const uint32_t ul = e - static_cast<uint32_t>(lead);
         if (ul < ulen) {
-            st_entry(J.suf + ustart + ul, stage[e + e / kBuildEPT]);
+            st_elem(J, J.suf, ustart + ul, stage[e + e / kBuildEPT]);
         }
     }
     // The next unit's first shared-memory writes (s_warp, stage) come after
@@ -500,7 +510,7 @@ __device__ __forceinline__ void build_unit_stream(const UnitJob &J, uint32_t u, 
             s_sufc[t] = acc;
             acc = umin64(acc, s_tmin[t]);
         }
-        J.bmin[u] = acc;  // block minimum
+        st_bmin(J, u, acc);  // block minimum
     }
     __syncthreads();
 
@@ -531,7 +541,7 @@ __device__ __forceinline__ void build_unit_stream(const UnitJob &J, uint32_t u, 
         for (int k = 0; k < kBuildEPT; ++k) {
             const uint32_t e = threadIdx.x + k * kBuildThreads;
             const uint32_t ul = static_cast<uint32_t>(tile_ul + e);
-            if (ul < ulen) st_entry(J.pre + ustart + ul, stage[e + e / kBuildEPT]);
+            if (ul < ulen) st_elem(J, J.pre, ustart + ul, stage[e + e / kBuildEPT]);
         }
         __syncthreads();
         run = ex_s;
@@ -545,7 +555,7 @@ __device__ __forceinline__ void build_unit_stream(const UnitJob &J, uint32_t u, 
         for (int k = 0; k < kBuildEPT; ++k) {
             const uint32_t e = threadIdx.x + k * kBuildThreads;
             const uint32_t ul = static_cast<uint32_t>(tile_ul + e);
-            if (ul < ulen) st_entry(J.suf + ustart + ul, stage[e + e / kBuildEPT]);
+            if (ul < ulen) st_elem(J, J.suf, ustart + ul, stage[e + e / kBuildEPT]);
         }
         // the next tile's first shared writes (s_warp in its CTA scan, then
         // stage) follow a barrier that every thread reaches after these reads

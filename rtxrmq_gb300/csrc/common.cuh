@@ -103,6 +103,35 @@ __device__ __forceinline__ uint32_t ld_u1(const float *p) {
 }
 #endif
 
+// Checked builds (-DRMQ_CHECKED=1), the engine's stand-in for a memory
+// sanitizer: every global index a kernel uses is range-checked first with
+// rmq_chk(in_range); a failed check is counted in this translation unit's
+// device counter and the access is skipped (no trap, no fault). Normal
+// builds compile rmq_chk to `true`.
+#ifndef RMQ_CHECKED
+#define RMQ_CHECKED 0
+#endif
+#ifdef __CUDACC__
+#if RMQ_CHECKED
+static __device__ unsigned long long g_rmq_violations = 0;
+__device__ __forceinline__ bool rmq_chk(bool in_range) {
+    if (!in_range) atomicAdd(&g_rmq_violations, 1ull);
+    return in_range;
+}
+// host reader of this translation unit's counter
+#define RMQ_VIOLATIONS_READER(name)                                                     \
+    unsigned long long name() {                                                         \
+        unsigned long long v = 0;                                                       \
+        if (cudaMemcpyFromSymbol(&v, g_rmq_violations, sizeof(v)) != cudaSuccess) v = ~0ull; \
+        return v;                                                                       \
+    }
+#else
+__device__ __forceinline__ bool rmq_chk(bool) { return true; }
+#define RMQ_VIOLATIONS_READER(name) \
+    unsigned long long name() { return 0; }
+#endif
+#endif
+
 // Exact unsigned division of x < 2^31 by a runtime divisor d >= 1:
 //   q = floor(x * m / 2^(31 + s)),  s = ceil(log2 d),  m = ceil(2^(31+s) / d).
 // With e = m*d - 2^(31+s) < d <= 2^s and x < 2^31 the error term

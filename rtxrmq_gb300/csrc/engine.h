@@ -63,6 +63,12 @@ cudaError_t occupancy_cached(K kernel, int threads, std::atomic<int> &cache, int
     return cudaSuccess;
 }
 
+// Checked builds: out-of-range accesses caught per translation unit.
+unsigned long long violations_build();
+unsigned long long violations_query();
+unsigned long long violations_batch();
+unsigned long long violations_persist();
+
 // ---- plain index (build.cu) ----
 struct BuildPlan {
     const float *A;

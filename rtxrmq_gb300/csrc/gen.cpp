@@ -70,10 +70,15 @@ void fill_queries(int32_t *out, int64_t q, int64_t n, int fixed_len, double mu, 
 
 }  // namespace
 
+namespace rmq {
+int set_error(int code, const char *fmt, ...);  // api.cu: status + message for rmq_last_error_string
+}
+using rmq::set_error;
+
 extern "C" {
 
 int rmq_gen_values_uniform(float *h_out, int64_t n, uint64_t seed) {
-    if (!h_out || n < 0) return RMQ_EINVAL;
+    if (!h_out || n < 0) return set_error(RMQ_EINVAL, "rmq_gen_values_uniform: NULL output or n < 0");
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         uint64_t s = stream_for(seed, static_cast<uint64_t>(i));
@@ -83,7 +88,7 @@ int rmq_gen_values_uniform(float *h_out, int64_t n, uint64_t seed) {
 }
 
 int rmq_gen_values_normal(float *h_out, int64_t n, double mean, double stddev, uint64_t seed) {
-    if (!h_out || n < 0) return RMQ_EINVAL;
+    if (!h_out || n < 0) return set_error(RMQ_EINVAL, "rmq_gen_values_normal: NULL output or n < 0");
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         uint64_t s = stream_for(seed, static_cast<uint64_t>(i));
@@ -93,7 +98,8 @@ int rmq_gen_values_normal(float *h_out, int64_t n, double mean, double stddev, u
 }
 
 int rmq_gen_values_int(float *h_out, int64_t n, int32_t range, uint64_t seed) {
-    if (!h_out || n < 0 || range <= 0) return RMQ_EINVAL;
+    if (!h_out || n < 0 || range <= 0)
+        return set_error(RMQ_EINVAL, "rmq_gen_values_int: NULL output, n < 0 or range <= 0");
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         uint64_t s = stream_for(seed, static_cast<uint64_t>(i));
@@ -103,9 +109,12 @@ int rmq_gen_values_int(float *h_out, int64_t n, int32_t range, uint64_t seed) {
 }
 
 int rmq_gen_queries(int32_t *h_out, int64_t q, int64_t n, int32_t lr, uint64_t seed) {
-    if (!h_out || q < 0 || n <= 0 || n > 0x7fffffffLL) return RMQ_EINVAL;
+    if (!h_out || q < 0 || n <= 0 || n > 0x7fffffffLL)
+        return set_error(RMQ_EINVAL, "rmq_gen_queries: NULL output, q < 0 or n outside [1, 2^31-1]");
     if (lr > 0) {
-        if (lr > n) return RMQ_EINVAL;
+        if (lr > n)
+            return set_error(RMQ_EINVAL, "rmq_gen_queries: fixed length lr=%d exceeds n=%lld", lr,
+                             static_cast<long long>(n));
         fill_queries(h_out, q, n, lr, 0.0, 0.0, false, seed);
         return RMQ_OK;
     }
@@ -124,13 +133,14 @@ int rmq_gen_queries(int32_t *h_out, int64_t q, int64_t n, int32_t lr, uint64_t s
         fill_queries(h_out, q, n, 0, std::log(sc), 0.3, false, seed);
         return RMQ_OK;
     }
-    default: return RMQ_EINVAL;
+    default: return set_error(RMQ_EINVAL, "rmq_gen_queries: lr=%d is not a length mode (> 0, -1 .. -5)", lr);
     }
 }
 
 int rmq_gen_queries_lognormal(int32_t *h_out, int64_t q, int64_t n, double mu, double sigma,
                               uint64_t seed) {
-    if (!h_out || q < 0 || n <= 0 || n > 0x7fffffffLL || !(sigma >= 0.0)) return RMQ_EINVAL;
+    if (!h_out || q < 0 || n <= 0 || n > 0x7fffffffLL || !(sigma >= 0.0))
+        return set_error(RMQ_EINVAL, "rmq_gen_queries_lognormal: bad arguments (q, n or sigma)");
     fill_queries(h_out, q, n, 0, mu, sigma, false, seed);
     return RMQ_OK;
 }

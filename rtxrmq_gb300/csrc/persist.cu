@@ -98,6 +98,8 @@ uint64_t header_hash(const FileHeader &h) {
 }
 
 }  // namespace
+RMQ_VIOLATIONS_READER(violations_persist)
+
 }  // namespace rmq
 
 using namespace rmq;

@@ -131,6 +131,8 @@ V1View view_of(const BuildPlan &p) {
     v.mpre = p.micro ? p.mpre : nullptr;
     v.msuf = p.micro ? p.msuf : nullptr;
     v.kmode = p.kmode;
+    v.levels = p.levels;
+    v.mlevels = p.micro ? p.mlevels : 0u;
     return v;
 }
 
@@ -143,6 +145,7 @@ cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInf
     o.val = a.val;
     o.idx = a.idx;
     o.invalid = a.invalid;
+    o.span = a.q;
     cudaError_t err;
     if (p.aligned) {
         int per_sm;
@@ -169,6 +172,7 @@ cudaError_t launch_probe_gather(const BuildPlan &p, const QueryArgs &a, const De
     o.val = a.val;
     o.idx = a.idx;
     o.invalid = nullptr;
+    o.span = a.q;
     int per_sm;
     cudaError_t err = occupancy(gather_kernel, &g_gather_per_sm, &per_sm);
     if (err != cudaSuccess) return err;
@@ -187,8 +191,11 @@ cudaError_t launch_query_scan(const float *A, uint32_t n, const QueryArgs &a,
     o.val = a.val;
     o.idx = a.idx;
     o.invalid = a.invalid;
+    o.span = a.q;
     scan_kernel<<<grid_size(a.q, kThreads, per_sm, dev), kThreads, 0, s>>>(A, n, o, a.q);
     return cudaGetLastError();
 }
+
+RMQ_VIOLATIONS_READER(violations_query)
 
 }  // namespace rmq

@@ -47,7 +47,21 @@ struct V1View {
     const Entry *mpre;  // in-micro-block prefix / suffix minima
     const Entry *msuf;
     uint32_t kmode;     // KeyMode: element type and minimum / maximum
+    uint32_t levels;    // sparse-table levels (st holds levels * nb entries)
+    uint32_t mlevels;   // micro-table levels (mst holds mlevels * nmicro entries)
 };
+
+// Range-checked accesses (rmq_chk, common.cuh): element loads by absolute
+// index into A, table entries by index into a table of `size` entries.
+__device__ __forceinline__ uint32_t ld_elem(const V1View &v, int64_t g) {
+    return rmq_chk(g >= 0 && g < v.limit) ? ld_u1(v.A + g) : 0u;
+}
+__device__ __forceinline__ uint4 ld_elem4(const V1View &v, int64_t g) {
+    return rmq_chk(g >= 0 && g + 3 < v.limit) ? ld_u4(v.A + g) : make_uint4(0u, 0u, 0u, 0u);
+}
+__device__ __forceinline__ Entry ld_entry(const Entry *t, uint64_t i, uint64_t size) {
+    return rmq_chk(i < size) ? t[i] : kEntryNone;
+}
 
 // Leftmost minimum of local A[a..b] (b - a < 32, at most 9 16-byte loads)
 // computed by one thread.
@@ -63,7 +77,7 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
             if (p <= ab) {
                 uint32_t w[4];
                 if (p + 3 < v.limit) {
-                    const uint4 f = ld_u4(v.A + p);
+                    const uint4 f = ld_elem4(v, p);
                     w[0] = f.x;
                     w[1] = f.y;
                     w[2] = f.z;
@@ -71,7 +85,7 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
                 } else {
 #pragma unroll
                     for (int c = 0; c < 4; ++c)
-                        w[c] = (p + c <= ab) ? ld_u1(v.A + p + c) : 0u;
+                        w[c] = (p + c <= ab) ? ld_elem(v, p + c) : 0u;
                 }
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
@@ -83,7 +97,7 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
         }
     } else {
         for (int64_t g = aa; g <= ab; ++g)
-            best = better(best, make_entry(ld_u1(v.A + g), static_cast<uint32_t>(g - v.off), v.kmode));
+            best = better(best, make_entry(ld_elem(v, g), static_cast<uint32_t>(g - v.off), v.kmode));
     }
     return best;
 }
@@ -96,12 +110,14 @@ template <bool ALIGNED>
 __device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
     const uint32_t ml = l >> 5, mr = r >> 5;
     if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
-    Entry e = better(v.msuf[l], v.mpre[r]);
+    Entry e = better(ld_entry(v.msuf, l, v.n), ld_entry(v.mpre, r, v.n));
     if (mr - ml >= 2u) {
         const uint32_t lo = ml + 1u, hi = mr - 1u;
         const int k = ilog2(hi - lo + 1u);
-        const Entry *lvl = v.mst + static_cast<size_t>(k) * v.nmicro;
-        e = better(e, better(lvl[lo], lvl[hi + 1u - (1u << k)]));
+        const uint64_t row = static_cast<uint64_t>(k) * v.nmicro;
+        const uint64_t size = static_cast<uint64_t>(v.mlevels) * v.nmicro;
+        e = better(e, better(ld_entry(v.mst, row + lo, size),
+                             ld_entry(v.mst, row + hi + 1u - (1u << k), size)));
     }
     return e;
 }
@@ -111,10 +127,12 @@ struct QueryOut {
     float *val;           // outputs aligned with Q, may be null
     int32_t *idx;         // may be null
     unsigned long long *invalid;
+    int64_t span;         // entries of Q / val / idx from these pointers on
 };
 
 __device__ __forceinline__ void put_bits_idx(const QueryOut &o, int64_t i, uint32_t bits,
                                              uint32_t idx) {
+    if (!rmq_chk(i >= 0 && i < o.span)) return;
     if (o.val) __stcs(reinterpret_cast<unsigned int *>(o.val) + i, bits);
     if (o.idx) __stcs(o.idx + i, static_cast<int32_t>(idx));
 }
@@ -124,6 +142,7 @@ __device__ __forceinline__ void put_result(const QueryOut &o, int64_t i, Entry e
 }
 
 __device__ __forceinline__ void put_invalid(const QueryOut &o, int64_t i) {
+    if (!rmq_chk(i >= 0 && i < o.span)) return;
     if (o.val) __stcs(reinterpret_cast<unsigned int *>(o.val) + i, 0x7fc00000u);
     if (o.idx) __stcs(o.idx + i, -1);
     if (o.invalid) atomicAdd(o.invalid, 1ull);
@@ -141,7 +160,7 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
         for (int64_t p = (al & ~int64_t(3)) + 4 * lane; p <= ar; p += 128) {
             uint32_t b[4];
             if (p + 3 < v.limit) {
-                const uint4 f = ld_u4(v.A + p);
+                const uint4 f = ld_elem4(v, p);
                 b[0] = f.x;
                 b[1] = f.y;
                 b[2] = f.z;
@@ -149,7 +168,7 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
             } else {
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    b[c] = (p + c <= ar) ? ld_u1(v.A + p + c) : 0u;
+                    b[c] = (p + c <= ar) ? ld_elem(v, p + c) : 0u;
             }
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
@@ -160,7 +179,7 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
         }
     } else {
         for (int64_t g = al + lane; g <= ar; g += 32)
-            best = better(best, make_entry(ld_u1(v.A + g), static_cast<uint32_t>(g - v.off), v.kmode));
+            best = better(best, make_entry(ld_elem(v, g), static_cast<uint32_t>(g - v.off), v.kmode));
     }
     // 64-bit minimum across the warp: the key word first, then the low word
     // among the lanes that hold that key
@@ -186,7 +205,7 @@ __device__ __forceinline__ void load_queries(const QueryOut &o, int64_t base, in
     for (int k = 0; k < QPT; ++k) {
         const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
         qq[k] = make_int2(0, 0);
-        if (i < q1) qq[k] = __ldcs(o.Q + i);
+        if (i < q1 && rmq_chk(i < o.span)) qq[k] = __ldcs(o.Q + i);
     }
 }
 
@@ -221,16 +240,17 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
             const bool use_suf = cross || (same && r[k] == bend);
             const bool use_pre = cross || (same && l[k] == bstart);
             scan[k] = same && !use_suf && !use_pre;
-            es[k] = use_suf ? v.suf[l[k]] : kEntryNone;
-            ep[k] = use_pre ? v.pre[r[k]] : kEntryNone;
+            es[k] = use_suf ? ld_entry(v.suf, l[k], v.n) : kEntryNone;
+            ep[k] = use_pre ? ld_entry(v.pre, r[k], v.n) : kEntryNone;
             ea[k] = kEntryNone;
             eb[k] = kEntryNone;
             if (cross && rB - lB >= 2u) {
                 const uint32_t lo = lB + 1u, hi = rB - 1u;
                 const int lev = ilog2(hi - lo + 1u);
-                const Entry *lvl = v.st + static_cast<size_t>(lev) * v.nb;
-                ea[k] = lvl[lo];
-                eb[k] = lvl[hi + 1u - (1u << lev)];
+                const uint64_t row = static_cast<uint64_t>(lev) * v.nb;
+                const uint64_t size = static_cast<uint64_t>(v.levels) * v.nb;
+                ea[k] = ld_entry(v.st, row + lo, size);
+                eb[k] = ld_entry(v.st, row + hi + 1u - (1u << lev), size);
             }
         }
         if (v.mst) {

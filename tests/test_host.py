@@ -257,3 +257,11 @@ def test_bench_reference_arm(native, oracle_lib):
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "RMQ/s"
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["steps"] == 3
+
+
+def test_normal_build_reports_not_checked(native):
+    """rmq_checked_violations answers RMQ_ENOTSUP outside the checked build."""
+    import ctypes as C
+    cnt = C.c_int64(-1)
+    assert native.rmq_checked_violations(C.byref(cnt)) == -5  # RMQ_ENOTSUP
+    assert cnt.value == 0
