@@ -117,12 +117,13 @@ template <bool ALIGNED>
 __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchParams P) {
     __shared__ Entry stage[kStageEntries];
     __shared__ uint64_t s_warp[kWarpSlots];
+    __shared__ uint32_t s_flag[2 * kBuildWarps];
     cg::grid_group grid = cg::this_grid();
 
     // A: units
     for (int32_t it = blockIdx.x; it < P.nbuild; it += gridDim.x) {
         const uint2 w = P.build[it];
-        build_unit<ALIGNED, kFloatMin>(unit_job(P, w.x), w.y, stage, s_warp);
+        build_unit<ALIGNED, kFloatMin>(unit_job(P, w.x), w.y, stage, s_warp, s_flag);
     }
     grid.sync();
 

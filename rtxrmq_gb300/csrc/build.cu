@@ -23,8 +23,9 @@ __global__ void __launch_bounds__(kBuildThreads, RMQ_BUILD_MINB)
 build_units_kernel(UnitJob J, uint32_t nunits) {
     __shared__ Entry stage[kStageEntries];
     __shared__ uint64_t s_warp[kWarpSlots];
+    __shared__ uint32_t s_flag[2 * kBuildWarps];
     for (uint32_t u = blockIdx.x; u < nunits; u += gridDim.x)
-        build_unit<ALIGNED, MODE>(J, u, stage, s_warp);
+        build_unit<ALIGNED, MODE>(J, u, stage, s_warp, s_flag);
 }
 
 template <bool ALIGNED>

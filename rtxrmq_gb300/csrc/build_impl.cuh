@@ -562,14 +562,153 @@ __device__ __forceinline__ void build_unit_stream(const UnitJob &J, uint32_t u, 
     }
 }
 
+// Segmented exclusive min-scans across the CTA of one value per thread in
+// both directions. Thread order (prefix): a thread with fp set starts a
+// segment, and its carry covers the threads of its segment before it. Reverse
+// order (suffix): a thread with fs set ends a segment. Pairs combine as
+// (F1, S1) + (F2, S2) = (F1 | F2, F2 ? S2 : min(S1, S2)), 2 later in scan
+// order; one barrier for both directions. A thread that starts (ends) a
+// segment ignores its prefix (suffix) carry itself.
+__device__ __forceinline__ void cta_segmented_min2(uint32_t fp, uint32_t fs, uint64_t v,
+                                                   uint64_t *s_warp, uint32_t *s_flag,
+                                                   uint64_t &xp, uint64_t &xs) {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    uint64_t sp = v, ss = v;
+    uint32_t gp = fp, gs = fs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t tsp = __shfl_up_sync(0xffffffffu, sp, o);
+        const uint32_t tgp = __shfl_up_sync(0xffffffffu, gp, o);
+        const uint64_t tss = __shfl_down_sync(0xffffffffu, ss, o);
+        const uint32_t tgs = __shfl_down_sync(0xffffffffu, gs, o);
+        if (lane >= o) {
+            sp = gp ? sp : umin64(tsp, sp);
+            gp |= tgp;
+        }
+        if (lane + o < 32) {
+            ss = gs ? ss : umin64(tss, ss);
+            gs |= tgs;
+        }
+    }
+    uint64_t ep = __shfl_up_sync(0xffffffffu, sp, 1);
+    uint32_t egp = __shfl_up_sync(0xffffffffu, gp, 1);
+    uint64_t es = __shfl_down_sync(0xffffffffu, ss, 1);
+    uint32_t egs = __shfl_down_sync(0xffffffffu, gs, 1);
+    if (lane == 0) { ep = ~0ull; egp = 0u; }
+    if (lane == 31) { es = ~0ull; egs = 0u; }
+    if (lane == 31) { s_warp[warp] = sp; s_flag[warp] = gp; }
+    if (lane == 0) { s_warp[kBuildWarps + warp] = ss; s_flag[kBuildWarps + warp] = gs; }
+    __syncthreads();
+    uint64_t ap = ~0ull, as = ~0ull;
+#pragma unroll
+    for (int w = 0; w < kBuildWarps; ++w) {
+        if (w < warp) ap = s_flag[w] ? s_warp[w] : umin64(ap, s_warp[w]);
+        const int wr = kBuildWarps - 1 - w;
+        if (wr > warp)
+            as = s_flag[kBuildWarps + wr] ? s_warp[kBuildWarps + wr] : umin64(as, s_warp[kBuildWarps + wr]);
+    }
+    xp = fp ? ~0ull : (egp ? ep : umin64(ap, ep));
+    xs = fs ? ~0ull : (egs ? es : umin64(as, es));
+}
+
+// One-tile unit whose blocks start at thread boundaries (the unit starts on
+// a 16-byte boundary and bs is a multiple of kBuildEPT; every unit of plain
+// arrays and of 4-aligned batched arrays): a thread's elements lie in one
+// block, so the thread-local scans need no segmentation and the CTA scan is
+// segmented by "this thread starts / ends a block" flags. Elements are
+// combined directly as index entries (no decode), so a unit of many small
+// blocks costs what a unit of one block does.
+template <bool ALIGNED, uint32_t MODE>
+__device__ __forceinline__ void build_unit_aligned(const UnitJob &J, uint32_t u, Entry *stage,
+                                                   uint64_t *s_warp, uint32_t *s_flag) {
+    const uint32_t G = J.U.G;
+    const uint32_t bs = J.bs;
+    const uint32_t ustart = u * G * bs;
+    const uint32_t ulen = min(ustart + G * bs, J.n) - ustart;
+    const int64_t base = J.off + ustart + static_cast<int64_t>(threadIdx.x) * kBuildEPT;
+    const uint32_t ul0 = threadIdx.x * kBuildEPT;
+
+    uint32_t bits[kBuildEPT];
+    if (ALIGNED && base + kBuildEPT <= J.limit) {
+#pragma unroll
+        for (int v = 0; v < kBuildEPT / 4; ++v) {
+            const uint4 f = ld_u4(J.A + base + 4 * v);
+            bits[4 * v + 0] = f.x;
+            bits[4 * v + 1] = f.y;
+            bits[4 * v + 2] = f.z;
+            bits[4 * v + 3] = f.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kBuildEPT; ++j) bits[j] = (ul0 + j < ulen) ? ld_u1(J.A + base + j) : 0u;
+    }
+    constexpr bool kFloat = (MODE == kFloatMin || MODE == kFloatMax);
+    Entry c[kBuildEPT];
+    uint64_t agg = kEntryNone;
+#pragma unroll
+    for (int j = 0; j < kBuildEPT; ++j) {
+        const uint32_t ul = ul0 + j;
+        const uint32_t nz = (kFloat && bits[j] == 0x80000000u) ? 1u : 0u;
+        const Entry e = (static_cast<uint64_t>(key_of(bits[j], MODE)) << 32) |
+                        ((ustart + ul) << 1) | nz;
+        c[j] = ul < ulen ? e : kEntryNone;
+        agg = umin64(agg, c[j]);
+    }
+    // block boundaries fall between threads: this thread starts a block when
+    // its first offset is a multiple of bs, ends one when the next is
+    const uint32_t r0 = ul0 - div31(ul0, J.dv) * bs;
+    const uint32_t fp = r0 == 0u ? 1u : 0u;
+    const uint32_t fs = (r0 + kBuildEPT == bs) ? 1u : 0u;
+    uint64_t ex_p, ex_s;
+    cta_segmented_min2(fp, fs, agg, s_warp, s_flag, ex_p, ex_s);
+
+    uint64_t run = ex_p;
+#pragma unroll
+    for (int j = 0; j < kBuildEPT; ++j) {
+        run = umin64(run, c[j]);
+        stage[threadIdx.x * (kBuildEPT + 1) + j] = run;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < kBuildEPT; ++k) {
+        const uint32_t e = threadIdx.x + k * kBuildThreads;
+        if (e < ulen) st_elem(J, J.pre, ustart + e, stage[e + e / kBuildEPT]);
+    }
+    {
+        // block minimum = prefix minimum at the block's last element
+        const uint32_t nblk = div31(ulen - 1u, J.dv) + 1u;
+        for (uint32_t b = threadIdx.x; b < nblk; b += kBuildThreads) {
+            const uint32_t last = min((b + 1u) * bs, ulen) - 1u;
+            st_bmin(J, u * G + b, stage[last + last / kBuildEPT]);
+        }
+    }
+    __syncthreads();
+    run = ex_s;
+#pragma unroll
+    for (int j = kBuildEPT - 1; j >= 0; --j) {
+        run = umin64(run, c[j]);
+        stage[threadIdx.x * (kBuildEPT + 1) + j] = run;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int k = 0; k < kBuildEPT; ++k) {
+        const uint32_t e = threadIdx.x + k * kBuildThreads;
+        if (e < ulen) st_elem(J, J.suf, ustart + e, stage[e + e / kBuildEPT]);
+    }
+}
+
 // Build unit `u`: one-tile units with the single-pass builder, others with
 // the tile-streaming one. The choice is uniform across the CTA.
 template <bool ALIGNED, uint32_t MODE>
 __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *stage,
-                                           uint64_t *s_warp) {
+                                           uint64_t *s_warp, uint32_t *s_flag) {
     int64_t t0;
     if (unit_tile<ALIGNED>(J, u, t0)) {
-        if (J.U.G > 1)
+        if (ALIGNED && t0 == J.off + static_cast<int64_t>(u) * J.U.G * J.bs &&
+            J.bs % kBuildEPT == 0)
+            build_unit_aligned<ALIGNED, MODE>(J, u, stage, s_warp, s_flag);
+        else if (J.U.G > 1)
             build_unit_tile<ALIGNED, MODE, true>(J, u, stage, s_warp);
         else
             build_unit_tile<ALIGNED, MODE, false>(J, u, stage, s_warp);
