@@ -351,6 +351,12 @@ def bench_batched(args, dev, stream, barrier):
                 "speedup_vs_per_array": pms / gms,
                 "default_bs_rmq_s": job_rate(q, nr, dms),
                 "per_array_matches_batched": match,
+                # algorithmic bytes of one step: the build reads each value once and
+                # writes its prefix / suffix entries (4 + 16 B per element), each
+                # query reads its pair and two random 32-B sectors and writes 8 B
+                # (80 B; table probes excluded); against the graph-launched step
+                "alg_bytes_per_step": int(w.lengths.sum()) * 20 + q * 80,
+                "alg_gbs": (int(w.lengths.sum()) * 20 + q * 80) / (gms / 1e3) / 1e9,
                 "launches_per_step": {"batched": 1, "per_array": "one build + level + query "
                                       "launch sequence per array"}})
     del dV, dQ, ov, oi
