@@ -1,13 +1,16 @@
 """GPU parity at the benchmark sizes.
 
-Plain RMQ at n = 1e8, q = 2^26 for every length mode, and the tie-heavy
+Plain RMQ at n = 1e8, q = 2^26 for every length mode, the tie-heavy
 configuration (n = 2^27 integers in [0,256), q = 2^26, fixed lengths
-1 .. 2^22). Brute force over 2^26 queries is out of reach on the CPU, so:
+1 .. 2^22) and the batched ragged configuration (4096 arrays, 2^26 queries):
+  * every answer is checked exactly against HRMQ, the reference's CPU
+    comparator restated in the oracle (hrmq_port.c, pinned to the
+    reference's own HRMQ outputs), in its leftmost-tie mode, run on all host
+    cores (brute force over 2^26 long ranges is out of reach on the CPU);
   * every answer is checked for size-independent properties: l <= idx <= r
     and the value is bit-identical to A[idx];
-  * a random sample of answers is checked exactly (index and value bits)
-    against the CPU oracle's restatement of the reference's block
-    decomposition, and for short lengths against BASE itself.
+  * a random sample is also checked against the oracle's restatement of the
+    reference's block decomposition, and for short lengths against BASE.
 """
 import numpy as np
 import pytest
@@ -41,10 +44,25 @@ def plain_data(cuda, native):
     return A, torch.from_numpy(A).to(cuda)
 
 
+@pytest.fixture(scope="module")
+def plain_hrmq(plain_data, oracle_lib):
+    h = oracle_lib.HRMQ(plain_data[0], strict=True)
+    yield h
+    h.close()
+
+
+def hrmq_exact(h, Q, v, i):
+    """Every answer against HRMQ (leftmost ties)."""
+    hv, hi = h.query(Q)
+    bad = np.nonzero(hi != i)[0]
+    assert bad.size == 0, f"{bad.size} index mismatches vs HRMQ; first q={bad[0]} (l,r)={tuple(Q[bad[0]])}"
+    np.testing.assert_array_equal(v.view(np.uint32), hv.view(np.uint32))
+
+
 # the block sizes the benchmark's sweep settles on per mode, and 4096
 @pytest.mark.parametrize("lr,bs", [(-1, 4096), (-1, 1 << 16), (-2, 4096), (-2, 1 << 14),
                                    (-3, 4096), (-3, 1024), (1024, 4096), (1024, 1024)])
-def test_plain_n1e8_q2e26(cuda, native, oracle_lib, plain_data, lr, bs):
+def test_plain_n1e8_q2e26(cuda, native, oracle_lib, plain_data, plain_hrmq, lr, bs):
     import torch
 
     import rtxrmq_gb300 as R
@@ -57,6 +75,7 @@ def test_plain_n1e8_q2e26(cuda, native, oracle_lib, plain_data, lr, bs):
         assert ix.invalid_count() == 0
     v, i = v.cpu().numpy(), i.cpu().numpy()
     check_properties(A, Q, v, i)
+    hrmq_exact(plain_hrmq, Q, v, i)
     sampled_exact(oracle_lib, A, Q, v, i, 1 << 14, 7)
     if lr in (-3, 1024):
         sampled_exact(oracle_lib, A, Q, v, i, 1 << 18, 8, base=True)
@@ -77,8 +96,9 @@ def test_tie_heavy_n2e27_q2e26(cuda, native, oracle_lib, length):
         torch.cuda.synchronize()
     v, i = v.cpu().numpy(), i.cpu().numpy()
     check_properties(A, Q, v, i)
-    # leftmost: nothing in [l, idx) equals the minimum (sampled; the sampled
-    # exact comparison below covers it too)
+    h = oracle_lib.HRMQ(A, strict=True)
+    hrmq_exact(h, Q, v, i)
+    h.close()
     sampled_exact(oracle_lib, A, Q, v, i, 1 << 13, 9)
     if length <= 1 << 10:
         sampled_exact(oracle_lib, A, Q, v, i, 1 << 16, 10, base=True)
@@ -90,8 +110,9 @@ def test_tie_heavy_n2e27_q2e26(cuda, native, oracle_lib, length):
 def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs):
     """Batched ragged configuration at full size (4096 arrays, lengths
     round(2^U) with U ~ U[8,22], 2^26 queries): every answer's properties,
-    and a sample exactly against BASE on the shared value buffer (a query
-    (l, r) of the array at offset o is the global query (o+l, o+r))."""
+    every answer exactly against HRMQ and a sample against BASE, both on the
+    shared value buffer (a query (l, r) of the array at offset o is the
+    global query (o+l, o+r))."""
     import torch
 
     from rtxrmq_gb300 import workloads as W
@@ -109,6 +130,12 @@ def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs):
     gi = i + off
     assert (gi >= G[:, 0]).all() and (gi <= G[:, 1]).all(), "index outside its range"
     np.testing.assert_array_equal(w.values[gi].view(np.uint32), v.view(np.uint32))
+    # every answer against HRMQ over the shared value buffer
+    h = oracle_lib.HRMQ(w.values, strict=True)
+    hv, hi = h.query(G.astype(np.int32))
+    h.close()
+    np.testing.assert_array_equal(gi, hi)
+    np.testing.assert_array_equal(v.view(np.uint32), hv.view(np.uint32))
     s = np.random.default_rng(12).integers(0, len(G), 1 << 14)
     ev, ei = oracle_lib.base_val(w.values, G[s]), oracle_lib.base_idx(w.values, G[s])
     np.testing.assert_array_equal(gi[s], ei)
