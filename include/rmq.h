@@ -128,13 +128,22 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
  * (Grace-Blackwell) -- the query kernel reads the queries and writes the
  * results in place over the host link (NVLink-C2C on GB300), with no staging
  * copies and no allocation. Otherwise the work is staged through device
- * memory in 4 Mi-query chunks on two internal streams (queries copied in or
- * read in place, results copied out while later chunks run); that path
- * allocates its staging (192 MB) and streams on its first call on a handle.
+ * memory in 4 Mi-query chunks on three internal streams (queries copied in,
+ * chunk kernels, results copied out while later chunks run; addressable
+ * buffers stay in place); that path allocates its staging (192 MB), streams
+ * and events on its first call on a handle, all or nothing.
  * Stream ordered with respect to `stream`: the results are in the host
  * buffers once `stream` has been synchronised. Calls on one handle from
  * several threads are serialised on the staged path. This is the end-to-end
  * form of the reference's timed loop plus its copy-out (src/rtx.h:150-159).
+ *
+ * Environment switches read by the library:
+ *   RTXRMQ_HOST_STAGED=1  every rmq_query_host buffer through staging
+ *   RTXRMQ_HOST_MODE=<m>  addressable host buffers through staging anyway:
+ *                         bit 0 the results, bit 1 the queries
+ *   RTXRMQ_FAIL_ALLOC=1   every device allocation of the library fails as
+ *                         out-of-memory (host-side fault injection for tests)
+ *   RTXRMQ_NVML_LIBRARY   path of the NVML library the power sampler opens
  */
 int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q,
                    float *h_val, int32_t *h_idx, rmq_stream_t stream);
