@@ -10,14 +10,27 @@
 // compute_min_blocks src/rtx.h:3-22).
 //
 // One CTA owns a "unit": one block when blocks are large, or G whole blocks
-// (G * bs <= 4096 elements) when they are small. A unit is streamed in
-// 4096-element tiles (16 consecutive elements per thread, 16-byte loads aligned
-// on absolute element indices): suffix pass right-to-left, then prefix pass
-// left-to-right (re-reading lines the suffix pass just brought into L2), each
-// tile a thread-local scan plus a CTA-wide scan, carried across tiles.
-// Results are staged in shared memory and written with coalesced stores.
+// (G * bs <= 4096 elements) when they are small. A tile is 4096 elements:
+// 16 consecutive elements per thread, 16-byte loads aligned on absolute
+// element indices, results staged in shared memory and written with
+// coalesced stores. Entries are the comparison composites of common.cuh. A
+// unit takes one of four paths (build_unit):
+//   build_unit_aligned  one tile, blocks starting at thread boundaries (the
+//                       unit on a 16-byte boundary, bs a multiple of 16):
+//                       one load, no per-element segmentation, one CTA scan
+//                       segmented by per-thread block start / end flags for
+//                       both directions;
+//   build_unit_tile     any other one-tile unit: one load, one CTA scan for
+//                       both directions, segmented by segment ranks in the
+//                       composite (below);
+//   build_unit_stream   one block of 2 .. kMaxStreamTiles tiles: per-tile
+//                       minima first, then every tile as a one-tile unit
+//                       with its prefix and suffix carries;
+//   build_unit_tiles    larger blocks: suffix pass right-to-left, then prefix
+//                       pass left-to-right, carried across tiles.
 //
-// Segmented scans without flags: every element becomes one 64-bit composite
+// Segmented scans without flags (build_unit_tile, build_unit_tiles): every
+// element becomes one 64-bit composite
 //   [segment rank | key(value) | local index | -0.0 bit]
 // whose unsigned minimum is the leftmost minimum. In the prefix direction
 // earlier blocks of the unit get a larger rank, in the suffix direction later
