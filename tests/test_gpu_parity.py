@@ -474,3 +474,85 @@ def test_allocation_failure_injection(cuda, native, oracle_lib, monkeypatch, tmp
     with R.RMQIndex.load(dA, tmp_path / "ix.rmq") as ix2:
         v, i = ix2.query(torch.from_numpy(Q).to(cuda))
         np.testing.assert_array_equal(i.cpu().numpy(), ei)
+
+
+def test_query_graph_capture(cuda, native, oracle_lib):
+    """rmq_query allocates nothing, so it can be captured in a CUDA graph
+    (after a first call has cached its launch configuration) and replayed on
+    new query contents."""
+    import torch
+
+    import oracle
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(21)
+    n = 200_000
+    A = rng.random(n).astype(np.float32)
+    dA = torch.from_numpy(A).to(cuda)
+    Q0 = R.gen_queries(50_000, n, -3, 1)
+    dQ = torch.from_numpy(Q0).to(cuda)
+    with R.RMQIndex(dA, 1024) as ix:
+        v = torch.empty(len(Q0), dtype=torch.float32, device=cuda)
+        i = torch.empty(len(Q0), dtype=torch.int32, device=cuda)
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            ix.query(dQ, out_val=v, out_idx=i, stream=s)  # warm: caches the launch shape
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            ix.query(dQ, out_val=v, out_idx=i)
+        for seed, lr in ((2, -1), (3, 1024), (4, -3)):
+            Q = R.gen_queries(len(Q0), n, lr, seed)
+            dQ.copy_(torch.from_numpy(Q).to(cuda))
+            g.replay()
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(i.cpu().numpy(), oracle.base_idx(A, Q))
+            np.testing.assert_array_equal(v.cpu().numpy().view(np.uint32),
+                                          oracle.base_val(A, Q).view(np.uint32))
+
+
+def test_concurrent_queries_one_handle(cuda, native, oracle_lib):
+    """A handle is immutable after its build: host threads may query it at
+    the same time on their own streams (device and host-buffer paths)."""
+    import threading
+
+    import torch
+
+    import oracle
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(22)
+    n = 300_000
+    A = rng.integers(0, 1000, n).astype(np.float32)
+    dA = torch.from_numpy(A).to(cuda)
+    sets = [R.gen_queries(40_000, n, lr, 30 + k) for k, lr in enumerate((-1, -3, 64, -2))]
+    want = [oracle.base_idx(A, Q) for Q in sets]
+    got = [None] * len(sets)
+    errors = []
+    with R.RMQIndex(dA, 2048) as ix:
+        def work(k):
+            try:
+                torch.cuda.set_device(cuda)
+                s = torch.cuda.Stream()
+                with torch.cuda.stream(s):
+                    if k % 2 == 0:
+                        v, i = ix.query(torch.from_numpy(sets[k]).to(cuda), stream=s)
+                        s.synchronize()
+                        got[k] = i.cpu().numpy()
+                    else:
+                        hv = np.empty(len(sets[k]), np.float32)
+                        hi = np.empty(len(sets[k]), np.int32)
+                        for _ in range(3):
+                            ix.query_host(sets[k], hv, hi, stream=s)
+                        s.synchronize()
+                        got[k] = hi
+            except Exception as e:  # surfaced below
+                errors.append(e)
+        threads = [threading.Thread(target=work, args=(k,)) for k in range(len(sets))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join(timeout=120)
+        assert not errors, errors
+        for k in range(len(sets)):
+            np.testing.assert_array_equal(got[k], want[k])
+        assert ix.invalid_count() == 0
