@@ -507,6 +507,26 @@ def main():
 
                 e2e_ms = time_steps(e2e, args.steps, args.warmup, stream, barrier)
                 torch.cuda.synchronize()
+                # the host link's ceiling for this traffic: the step's bytes in
+                # and out copied at the same time on two streams (copy engines;
+                # kernel loads and stores over NVLink-C2C reach the same rate)
+                dQc = torch.empty_like(dQ)
+                dR = torch.empty(2 * q, dtype=torch.int32, device=dev)
+                hR = torch.empty(2 * q, dtype=torch.int32).pin_memory()
+                s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+                def link():
+                    s_in.wait_stream(stream)
+                    s_out.wait_stream(stream)
+                    with torch.cuda.stream(s_in):
+                        dQc.copy_(hQ, non_blocking=True)
+                    with torch.cuda.stream(s_out):
+                        hR.copy_(dR, non_blocking=True)
+                    stream.wait_stream(s_in)
+                    stream.wait_stream(s_out)
+
+                link_ms = time_steps(link, max(3, args.steps // 2), 2, stream, barrier)
+                del dQc, dR, hR
                 ix.query(dQ, out_val=out_v, out_idx=out_i)
                 torch.cuda.synchronize()
                 ok = (np.array_equal(hI.numpy(), out_i.cpu().numpy()) and
@@ -515,7 +535,13 @@ def main():
                               "h2d_bytes_per_step": int(Q.nbytes),
                               "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
                               "ms_per_step": e2e_ms, "path": "rmq_query_host, pinned host buffers read and written in place",
-                              "matches_device_path": bool(ok)}
+                              "matches_device_path": bool(ok),
+                              "link_ceiling": {"ms_per_step": link_ms,
+                                               "rmq_s": job_rate(q, world, link_ms),
+                                               "gbs_per_direction": Q.nbytes / (link_ms / 1e3) / 1e9,
+                                               "frac": link_ms / e2e_ms,
+                                               "how": "the step's query bytes in and result bytes out "
+                                                      "copied concurrently (pinned, two streams)"}}
                 del hQ, hV, hI
             if lr == -1:
                 # random-access ceiling on this index: rmq_probe_gather has the
