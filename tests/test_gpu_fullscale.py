@@ -142,3 +142,42 @@ def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs):
     np.testing.assert_array_equal(v[s].view(np.uint32), ev.view(np.uint32))
     del dV, dQ
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("micro", [True, False])
+def test_maximum_size_n2e31(cuda, native, oracle_lib, micro):
+    """The largest supported array, n = 2^31 - 1 (indices are int32): build
+    with and without the sub-block level, 2^22 queries of every length mode
+    plus queries touching the last elements; every answer's properties,
+    short ranges exactly against BASE, long ranges near the end against the
+    GPU brute force (alg 2 / 102)."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = 2**31 - 1
+    A = R.gen_values_uniform(n, 77)
+    dA = torch.from_numpy(A).to(cuda)
+    parts = [R.gen_queries(1 << 20, n, lr, 40 + k) for k, lr in enumerate((-1, -2, -3, 32))]
+    tail = np.array([[n - 1, n - 1], [n - 2, n - 1], [n - 1000, n - 1], [0, n - 1],
+                     [n - (1 << 20), n - 1], [n - 40, n - 33]], np.int32)
+    Q = np.concatenate(parts + [tail])
+    dQ = torch.from_numpy(Q).to(cuda)
+    with R.RMQIndex(dA, 0, micro=micro) as ix:  # default bs = 2^15
+        assert ix.info()["n"] == n
+        v, i = ix.query(dQ)
+        torch.cuda.synchronize()
+        assert ix.invalid_count() == 0
+    v, i = v.cpu().numpy(), i.cpu().numpy()
+    check_properties(A, Q, v, i)
+    short = np.nonzero(Q[:, 1] - Q[:, 0] < 4096)[0]
+    sel = short[np.random.default_rng(3).integers(0, len(short), 1 << 16)]
+    np.testing.assert_array_equal(i[sel], oracle_lib.base_idx(A, Q[sel]))
+    # ranges at the end of the array against the GPU brute force (one thread
+    # per query), the whole array against numpy's first-occurrence argmin
+    first = len(Q) - len(tail)
+    sub = np.array([first + k for k in range(len(tail)) if k != 3])
+    bi = R.gpu_rmq_basic_idx(n, len(sub), dA, torch.from_numpy(Q[sub]).to(cuda))
+    np.testing.assert_array_equal(i[sub], bi)
+    assert i[first + 3] == int(np.argmin(A))
+    del dA, dQ
+    torch.cuda.empty_cache()
