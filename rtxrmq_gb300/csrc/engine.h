@@ -16,7 +16,8 @@ namespace rmq {
 
 // Records a message for rmq_last_error_string() and returns `code`.
 int set_error(int code, const char *fmt, ...);
-// Converts a CUDA error into RMQ_ECUDA with the call site in the message.
+// Converts a CUDA error into RMQ_ECUDA (RMQ_ENOMEM for an allocation
+// failure) with the call site in the message.
 int cuda_fail(cudaError_t err, const char *what);
 
 // Device properties the launchers need, cached per device.

@@ -11,8 +11,12 @@
 //   full blocks between  -> two sparse-table entries (L2-resident)
 // A query inside one block (the reference's single-ray case,
 // src/rtx_kernels.cu:116-135) is answered from pre/suf when it touches a
-// block edge, otherwise by a warp-cooperative scan of A[l..r] that reduces
-// order-preserving keys with __reduce_min_sync.
+// block edge; otherwise through the sub-block level when the index has one
+// (32-element micro-blocks: msuf[l], mpre[r] and two micro-table entries, or
+// one thread's scan of a single 128-byte line), and by a warp-cooperative
+// scan of A[l..r] reducing the composites with __reduce_min_sync when it
+// does not. All comparisons are unsigned minima of the composites of
+// common.cuh; only the final answer is decoded.
 //
 // Differences from the reference kept on purpose: ties between rays are
 // resolved leftmost (the reference compares rays with strict `<` in the
