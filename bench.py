@@ -336,6 +336,9 @@ def bench_batched(args, dev, stream, barrier):
         ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
         g = graph_of(fn, stream)
         gms = time_steps(g.replay, args.steps, args.warmup, stream, barrier)
+        # the two halves: build every array, then answer from the built index
+        bms = time_steps(lambda: b.build(dV), args.steps, args.warmup, stream, barrier)
+        qms = time_steps(lambda: b.query(dV, dQ, ov, oi), args.steps, args.warmup, stream, barrier)
         v1, i1 = ov.clone(), oi.clone()
         pms = time_steps(lambda: b.run_per_array(dV, dQ, ov, oi), max(2, args.steps // 3), 1,
                          stream, barrier)
@@ -351,6 +354,8 @@ def bench_batched(args, dev, stream, barrier):
                 "speedup_vs_per_array": pms / gms,
                 "default_bs_rmq_s": job_rate(q, nr, dms),
                 "per_array_matches_batched": match,
+                "build_only_ms": bms, "query_only_ms": qms,
+                "query_only_rmq_s": job_rate(q, nr, qms),
                 # algorithmic bytes of one step: the build reads each value once and
                 # writes its prefix / suffix entries (4 + 16 B per element), each
                 # query reads its pair and two random 32-B sectors and writes 8 B

@@ -283,6 +283,20 @@ int rmq_batch_run(rmq_batch_t *b, const float *d_vals,
                   const int32_t *d_queries, float *d_val, int32_t *d_idx,
                   rmq_stream_t stream);
 
+/*
+ * The two halves of rmq_batch_run, for arrays that stay the same while the
+ * queries change: rmq_batch_build builds every array's index in the plan's
+ * workspace (one cooperative launch, phases build + tables);
+ * rmq_batch_query answers the plan's queries from that index (one
+ * cooperative launch, query phase only). rmq_batch_query needs a build
+ * (rmq_batch_build or rmq_batch_run) enqueued earlier on the same d_vals
+ * (RMQ_EINVAL otherwise); the values must not change in between. Both
+ * allocate nothing and can be captured in a CUDA graph.
+ */
+int rmq_batch_build(rmq_batch_t *b, const float *d_vals, rmq_stream_t stream);
+int rmq_batch_query(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
+                    float *d_val, int32_t *d_idx, rmq_stream_t stream);
+
 /* The same results through the plain path: per array one rmq_build-style
  * launch sequence and one rmq_query-style launch (comparison baseline). */
 int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals,

@@ -74,6 +74,8 @@ SIGNATURES = {
     "rmq_batch_create": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
     "rmq_batch_run": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_run_per_array": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "rmq_batch_build": (C.c_int, [_vp, _vp, _vp]),
+    "rmq_batch_query": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_scatter_grad": (C.c_int, [_vp, _vp, _vp, _vp, _i32, _vp]),
     "rmq_batch_info": (C.c_int, [_vp, C.POINTER(rmq_batch_info_t)]),
     "rmq_batch_invalid_count": (C.c_int, [_vp, _vp, C.POINTER(_i64)]),

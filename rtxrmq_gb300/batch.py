@@ -90,6 +90,20 @@ class RMQBatch:
                                    _stream(stream)))
         return v, i
 
+    def build(self, vals, stream=None) -> None:
+        """Build every array's index (rmq_batch_build); queries then run
+        with ``query`` as long as the values stay the same."""
+        check(load().rmq_batch_build(self._h, _dptr(vals), _stream(stream)))
+
+    def query(self, vals, queries, out_val=None, out_idx=None, *, values=True, indices=True,
+              stream=None):
+        """Answer the plan's queries from the last build on ``vals``
+        (rmq_batch_query), one cooperative launch."""
+        v, i = self._out(queries, out_val, out_idx, values, indices)
+        check(load().rmq_batch_query(self._h, _dptr(vals), _dptr(queries), _dptr(v), _dptr(i),
+                                     _stream(stream)))
+        return v, i
+
     def run_per_array(self, vals, queries, out_val=None, out_idx=None, *, values=True,
                       indices=True, stream=None):
         """Same results through the plain path, one launch sequence per array."""

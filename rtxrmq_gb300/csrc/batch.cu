@@ -71,6 +71,7 @@ struct BatchParams {
     const uint4 *qitems;
     int32_t nqitems;
     int64_t total_q;  // one past the last query any array owns
+    uint32_t phases;  // bit 0 build units, bit 1 table levels, bit 2 queries
 };
 
 __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchArray &a) {
@@ -121,14 +122,14 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
     cg::grid_group grid = cg::this_grid();
 
     // A: units
-    for (int32_t it = blockIdx.x; it < P.nbuild; it += gridDim.x) {
+    for (int32_t it = (P.phases & 1u) ? blockIdx.x : P.nbuild; it < P.nbuild; it += gridDim.x) {
         const uint2 w = P.build[it];
         build_unit<ALIGNED, kFloatMin>(unit_job(P, w.x), w.y, stage, s_warp, s_flag);
     }
     grid.sync();
 
     // B: sparse-table levels
-    for (int k = 1; k < P.maxlev; ++k) {
+    for (int k = 1; (P.phases & 2u) && k < P.maxlev; ++k) {
         for (int32_t it = P.lvl_start[k] + blockIdx.x; it < P.lvl_start[k + 1]; it += gridDim.x) {
             const uint4 w = P.lvl[it];
             const BatchArray &a = P.arrays[w.x];
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
     }
 
     // C: queries
-    for (int32_t it = blockIdx.x; it < P.nqitems; it += gridDim.x) {
+    for (int32_t it = (P.phases & 4u) ? blockIdx.x : P.nqitems; it < P.nqitems; it += gridDim.x) {
         const uint4 w = P.qitems[it];
         const BatchArray a = P.arrays[w.x];
         const V1View v = batch_view(P, a);
@@ -197,6 +198,7 @@ struct rmq_batch {
     size_t ws_bytes;
     BatchParams P;       // device pointers filled, per-run fields left empty
     int32_t bucket_bs[RMQ_BATCH_BUCKETS];
+    const float *built_vals;  // values of the last build enqueued on this plan
 };
 
 namespace {
@@ -228,6 +230,7 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
     if (!b) return set_error(RMQ_ENOMEM, "rmq_batch_create: host allocation failed");
     b->narrays = narrays;
     b->device = dev.device;
+    b->built_vals = nullptr;
     b->limit = 0;
     b->total_q = 0;
     b->mem = nullptr;
@@ -347,13 +350,13 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
 }
 
 static int batch_args(const rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
-                      float *d_val, int32_t *d_idx, const char *who) {
+                      float *d_val, int32_t *d_idx, const char *who, bool with_queries = true) {
     if (!b) return set_error(RMQ_EINVAL, "%s: batch is NULL", who);
     if (!d_vals || reinterpret_cast<uintptr_t>(d_vals) % 4)
         return set_error(RMQ_EINVAL, "%s: d_vals NULL or not 4-byte aligned", who);
-    if (b->total_q > 0 && (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8))
+    if (with_queries && b->total_q > 0 && (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8))
         return set_error(RMQ_EINVAL, "%s: d_queries NULL or not 8-byte aligned", who);
-    if (b->total_q > 0 && !d_val && !d_idx)
+    if (with_queries && b->total_q > 0 && !d_val && !d_idx)
         return set_error(RMQ_EINVAL, "%s: both outputs are NULL", who);
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
@@ -364,33 +367,60 @@ static int batch_args(const rmq_batch_t *b, const float *d_vals, const int32_t *
     return RMQ_OK;
 }
 
-int rmq_batch_run(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries, float *d_val,
-                  int32_t *d_idx, rmq_stream_t stream) {
-    NvtxRange nvtx_range("rmq_batch_run");
-    int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_run");
-    if (rc) return rc;
+// One cooperative launch of batch_kernel running the given phases.
+static int launch_batch(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,
+                        float *d_val, int32_t *d_idx, rmq_stream_t stream, uint32_t phases,
+                        const char *who) {
     DeviceInfo dev;
-    rc = device_info(&dev);
+    int rc = device_info(&dev);
     if (rc) return rc;
     BatchParams P = b->P;
     P.A = d_vals;
     P.Q = reinterpret_cast<const int2 *>(d_queries);
     P.val = d_val;
     P.idx = d_idx;
+    P.phases = phases;
     const bool aligned = reinterpret_cast<uintptr_t>(d_vals) % 16 == 0;
     void *kern = aligned ? reinterpret_cast<void *>(batch_kernel<true>)
                          : reinterpret_cast<void *>(batch_kernel<false>);
     int per_sm;
     cudaError_t err = aligned ? occupancy_cached(batch_kernel<true>, kThreads, g_batch_per_sm[1], per_sm)
                               : occupancy_cached(batch_kernel<false>, kThreads, g_batch_per_sm[0], per_sm);
-    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run: occupancy");
+    if (err != cudaSuccess) return cuda_fail(err, who);
     // a cooperative launch needs every CTA resident
-    if (per_sm < 1) return set_error(RMQ_ENOTSUP, "rmq_batch_run: kernel cannot be resident");
+    if (per_sm < 1) return set_error(RMQ_ENOTSUP, "%s: kernel cannot be resident", who);
     const unsigned grid = static_cast<unsigned>(dev.sms * per_sm);
     void *args[] = {&P};
     err = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, stream);
-    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run: cooperative launch");
+    if (err != cudaSuccess) return cuda_fail(err, who);
+    if (phases & 1u) b->built_vals = d_vals;
     return RMQ_OK;
+}
+
+int rmq_batch_run(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries, float *d_val,
+                  int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_batch_run");
+    const int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_run");
+    if (rc) return rc;
+    return launch_batch(b, d_vals, d_queries, d_val, d_idx, stream, 7u, "rmq_batch_run");
+}
+
+int rmq_batch_build(rmq_batch_t *b, const float *d_vals, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_batch_build");
+    const int rc = batch_args(b, d_vals, nullptr, nullptr, nullptr, "rmq_batch_build", false);
+    if (rc) return rc;
+    return launch_batch(b, d_vals, nullptr, nullptr, nullptr, stream, 3u, "rmq_batch_build");
+}
+
+int rmq_batch_query(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries, float *d_val,
+                    int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_batch_query");
+    const int rc = batch_args(b, d_vals, d_queries, d_val, d_idx, "rmq_batch_query");
+    if (rc) return rc;
+    if (b->built_vals != d_vals)
+        return set_error(RMQ_EINVAL, "rmq_batch_query: the plan was not built (rmq_batch_build or "
+                                     "rmq_batch_run) on these values");
+    return launch_batch(b, d_vals, d_queries, d_val, d_idx, stream, 4u, "rmq_batch_query");
 }
 
 int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *d_queries,

@@ -199,3 +199,55 @@ def test_autotune(cuda, native, oracle_lib, tmp_path):
         assert b.info()["bucket_bs"][:32] == cfg
         v, i = b.run(dA, dQ)
         np.testing.assert_array_equal(i.cpu().numpy()[own], ei[own])
+
+
+def test_batch_build_once_query_many(cuda, native, oracle_lib):
+    """rmq_batch_build + rmq_batch_query: one build, several query sets of the
+    plan's layout (also captured in a CUDA graph); a query without a build on
+    the same values is refused."""
+    import torch
+
+    import oracle
+    import rtxrmq_gb300 as R
+    from rtxrmq_gb300.batch import RMQBatch
+    rng = np.random.default_rng(31)
+    lengths = rng.integers(1, 20000, 64).astype(np.int64)
+    starts = np.concatenate([[0], np.cumsum(lengths)[:-1]]).astype(np.int64)
+    qcounts = rng.integers(1, 2000, 64).astype(np.int64)
+    qstarts = np.concatenate([[0], np.cumsum(qcounts)[:-1]]).astype(np.int64)
+    V = rng.random(int(lengths.sum())).astype(np.float32)
+    dV = torch.from_numpy(V).to(cuda)
+    off = np.repeat(starts, qcounts)
+
+    def queries(seed, lr):
+        return np.concatenate([R.gen_queries(int(c), int(m), lr, seed + k)
+                               for k, (m, c) in enumerate(zip(lengths, qcounts))])
+
+    with RMQBatch(starts, lengths, qstarts, qcounts, [256] * 32) as b:
+        Q0 = queries(1, -3)
+        dQ = torch.from_numpy(Q0).to(cuda)
+        with pytest.raises(R.RMQError, match="not built"):
+            b.query(dV, dQ)
+        b.build(dV)
+        for seed, lr in ((1, -3), (2, -1), (3, 50)):
+            Q = queries(seed, lr)
+            v, i = b.query(dV, torch.from_numpy(Q).to(cuda))
+            G = Q.astype(np.int64) + off[:, None]
+            np.testing.assert_array_equal(i.cpu().numpy() + off, oracle.base_idx(V, G))
+        other = dV.clone()
+        with pytest.raises(R.RMQError, match="not built"):
+            b.query(other, dQ)
+        # the query half captured in a graph and replayed on new query contents
+        v = torch.empty(len(Q0), dtype=torch.float32, device=cuda)
+        i = torch.empty(len(Q0), dtype=torch.int32, device=cuda)
+        b.query(dV, dQ, v, i)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            b.query(dV, dQ, v, i)
+        Q = queries(7, -2)
+        dQ.copy_(torch.from_numpy(Q).to(cuda))
+        g.replay()
+        torch.cuda.synchronize()
+        G = Q.astype(np.int64) + off[:, None]
+        np.testing.assert_array_equal(i.cpu().numpy() + off, oracle.base_idx(V, G))
