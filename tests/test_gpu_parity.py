@@ -556,3 +556,33 @@ def test_concurrent_queries_one_handle(cuda, native, oracle_lib):
         for k in range(len(sets)):
             np.testing.assert_array_equal(got[k], want[k])
         assert ix.invalid_count() == 0
+
+
+def test_cli_csv_nb_and_power(native, tmp_path):
+    """The CLI's --save-time row has the reference's 13 columns
+    (dev,alg,reps,n,bs,q,lr,t,q/s,ns/q,construction,outbuffer,tempbuffer,
+    scripts/perf-benchmark.sh:30) with bs resolved from --nb as n / nb
+    (src/tools.h:129-132); --save-power writes a power table and prints
+    RMQs/J (or warns and continues where NVML is unavailable)."""
+    import subprocess
+    cli = Path(__file__).resolve().parent.parent / "rtxrmq_gb300" / "_lib" / "rtxrmq"
+    csv = tmp_path / "t.csv"
+    pw = tmp_path / "p.dat"
+    n, q, nb = 1_000_003, 262_144, 512
+    for alg in ("5", "105"):
+        r = subprocess.run([str(cli), str(n), str(q), "-1", alg, "--nb", str(nb), "--reps", "3",
+                            f"--save-time={csv}", f"--save-power={pw}"],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "RMQs/J" in r.stdout or "power sampling unavailable" in r.stderr
+    rows = [line.split(",") for line in csv.read_text().splitlines()]
+    assert len(rows) == 2
+    for row in rows:
+        assert len(row) == 13
+        dev, alg, reps, n_, bs, q_, lr = row[:7]
+        assert (int(reps), int(n_), int(bs), int(q_), int(lr)) == (3, n, n // nb, q, -1)
+        t, qps, nsq, constr = (float(x) for x in row[7:11])
+        assert t > 0 and qps > 0 and nsq > 0 and constr > 0
+        assert abs(qps * nsq / 1e9 - 1.0) < 1e-3   # q/s and ns/q are reciprocal
+    if pw.exists():
+        assert pw.stat().st_size > 0
