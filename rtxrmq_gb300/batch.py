@@ -50,6 +50,22 @@ def _dptr(t):
     return t.data_ptr()
 
 
+def _vals(t):
+    """Device pointer of the flat float32 value buffer."""
+    import torch
+    if t.dtype != torch.float32 or t.dim() != 1:
+        raise TypeError("values must be a 1-D float32 CUDA tensor")
+    return _dptr(t)
+
+
+def _queries(t):
+    """Device pointer of the int32 [q, 2] query tensor."""
+    import torch
+    if t.dtype != torch.int32 or t.dim() != 2 or t.shape[1] != 2:
+        raise TypeError("queries must be an int32 CUDA tensor of shape [q, 2]")
+    return _dptr(t)
+
+
 class RMQBatch:
     """A planned batch: array i is values[starts[i] : starts[i] + lengths[i]]
     and owns queries[qstarts[i] : qstarts[i] + qcounts[i]] (array-local
@@ -86,21 +102,21 @@ class RMQBatch:
             stream=None):
         """Build + answer everything in one cooperative launch."""
         v, i = self._out(queries, out_val, out_idx, values, indices)
-        check(load().rmq_batch_run(self._h, _dptr(vals), _dptr(queries), _dptr(v), _dptr(i),
+        check(load().rmq_batch_run(self._h, _vals(vals), _queries(queries), _dptr(v), _dptr(i),
                                    _stream(stream)))
         return v, i
 
     def build(self, vals, stream=None) -> None:
         """Build every array's index (rmq_batch_build); queries then run
         with ``query`` as long as the values stay the same."""
-        check(load().rmq_batch_build(self._h, _dptr(vals), _stream(stream)))
+        check(load().rmq_batch_build(self._h, _vals(vals), _stream(stream)))
 
     def query(self, vals, queries, out_val=None, out_idx=None, *, values=True, indices=True,
               stream=None):
         """Answer the plan's queries from the last build on ``vals``
         (rmq_batch_query), one cooperative launch."""
         v, i = self._out(queries, out_val, out_idx, values, indices)
-        check(load().rmq_batch_query(self._h, _dptr(vals), _dptr(queries), _dptr(v), _dptr(i),
+        check(load().rmq_batch_query(self._h, _vals(vals), _queries(queries), _dptr(v), _dptr(i),
                                      _stream(stream)))
         return v, i
 
@@ -108,7 +124,7 @@ class RMQBatch:
                       indices=True, stream=None):
         """Same results through the plain path, one launch sequence per array."""
         v, i = self._out(queries, out_val, out_idx, values, indices)
-        check(load().rmq_batch_run_per_array(self._h, _dptr(vals), _dptr(queries), _dptr(v),
+        check(load().rmq_batch_run_per_array(self._h, _vals(vals), _queries(queries), _dptr(v),
                                              _dptr(i), _stream(stream)))
         return v, i
 

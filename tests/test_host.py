@@ -265,3 +265,17 @@ def test_normal_build_reports_not_checked(native):
     cnt = C.c_int64(-1)
     assert native.rmq_checked_violations(C.byref(cnt)) == -5  # RMQ_ENOTSUP
     assert cnt.value == 0
+
+
+def test_batch_argument_types(native):
+    """The batched form refuses values that are not float32 and queries that
+    are not int32 [q, 2] before anything reaches the device."""
+    import torch
+
+    from rtxrmq_gb300 import batch as B
+    with pytest.raises(TypeError):
+        B._vals(torch.zeros(4, dtype=torch.float64))
+    with pytest.raises(TypeError):
+        B._queries(torch.zeros((4, 2), dtype=torch.int64))
+    with pytest.raises(TypeError):
+        B._queries(torch.zeros((4, 3), dtype=torch.int32))
