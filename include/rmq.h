@@ -253,7 +253,8 @@ int rmq_checked_violations(int64_t *count);
  * no structure, and every query it owns is invalid (index -1, value NaN,
  * counted by rmq_batch_invalid_count). Arrays are grouped into size buckets
  * floor(log2 length); h_bucket_bs[bucket] (RMQ_BATCH_BUCKETS entries, or
- * NULL; <= 0 means default) is the block size of that bucket, as chosen by
+ * NULL; <= 0 means the default: 64 below 2^17 elements, 256 above) is the
+ * block size of that bucket, as chosen by
  * rmq_batch_autotune.
  * ---------------------------------------------------------------------- */
 #define RMQ_BATCH_BUCKETS 32

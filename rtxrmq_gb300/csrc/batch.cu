@@ -206,8 +206,11 @@ namespace {
 int bucket_of(int64_t n) { return n <= 1 ? 0 : ilog2(static_cast<uint32_t>(n)); }
 
 int64_t default_bs(int64_t n) {
-    // short arrays: one block per 1024 elements; long arrays: 4096
-    return n <= (1 << 14) ? 1024 : 4096;
+    // Without autotuning: small blocks, so that a query inside one block is
+    // a short warp scan (the batched index has no sub-block level) and the
+    // sparse table does the rest; 64 below 2^17 elements, 256 above (what
+    // the autotuner picks for the ragged benchmark, within 5% of it there).
+    return n < (1 << 17) ? 64 : 256;
 }
 
 }  // namespace
