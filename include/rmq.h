@@ -92,7 +92,7 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
               rmq_handle_t **out);
 
 /*
- * rmq_build with options. When bs is a multiple of 32 (and >= 64) the index
+ * rmq_build with options. When bs >= 64 the index
  * also gets a sub-block level -- prefix and suffix minima inside 32-element
  * micro-blocks (16 more bytes per element) and a sparse table over the
  * micro-block minima, truncated to windows shorter than one block -- so

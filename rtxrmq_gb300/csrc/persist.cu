@@ -19,7 +19,7 @@ namespace rmq {
 namespace {
 
 constexpr char kMagic[16] = "RTXRMQ-GB300-IX";
-constexpr uint32_t kVersion = 2;  // 2: entries are comparison composites
+constexpr uint32_t kVersion = 3;  // 2: entries are comparison composites; 3: sub-block level for every bs >= 64
 constexpr size_t kIoChunk = size_t(64) << 20;
 
 struct FileHeader {

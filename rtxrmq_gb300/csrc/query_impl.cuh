@@ -43,9 +43,9 @@ struct V1View {
     const Entry *pre;
     const Entry *suf;
     const Entry *st;
-    // sub-block level: 32-element micro-blocks (local index / 32); null when
-    // the block size is not a multiple of 32 (same-block queries then use the
-    // warp-cooperative scan)
+    // sub-block level: 32-element micro-blocks (local index / 32), whatever
+    // the block size; null when the index has none (same-block queries then
+    // use the warp-cooperative scan)
     const Entry *mst;
     uint32_t nmicro;
     const Entry *mpre;  // in-micro-block prefix / suffix minima

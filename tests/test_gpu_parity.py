@@ -20,14 +20,14 @@ def bits(x):
 
 def run_index(cuda, A, Q, bs, values=True, indices=True, micro=True):
     """Build + query; micro=False forces the warp-scan path for queries
-    inside one block (micro=True uses the sub-block level when bs % 32 == 0)."""
+    inside one block (micro=True uses the sub-block level for every bs >= 64)."""
     import torch
 
     import rtxrmq_gb300 as R
     dA = torch.from_numpy(np.ascontiguousarray(A, dtype=np.float32)).to(cuda)
     dQ = torch.from_numpy(np.ascontiguousarray(Q, dtype=np.int32)).to(cuda)
     with R.RMQIndex(dA, bs, micro=micro) as ix:
-        if micro and bs >= 64 and bs % 32 == 0 and bs <= len(A):
+        if micro and bs >= 64 and bs <= len(A):
             assert ix.info()["micro_levels"] > 0
         v, i = ix.query(dQ, values=values, indices=indices)
         torch.cuda.synchronize()
