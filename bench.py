@@ -582,6 +582,20 @@ def main():
             ix.close()
             results[name] = res
             del dQ
+        # the reference's own block sizes: its benchmark scripts pass --nb 512
+        # (lr=-1, -2) and --nb 8192 (lr=-3), bs = n / nb
+        # (scripts/perf-fulltest.sh:49-58, src/tools.h:129-132)
+        ref_nb = {}
+        if modes and not args.bs:
+            for name, lr, nb in (("lr=-1", -1, 512), ("lr=-2", -2, 512), ("lr=-3", -3, 8192)):
+                bs = R.bs_from_nb(n, nb)
+                Q = R.gen_queries(q, n, lr, rank_seed(SEED, rank, lr))
+                dQ = torch.from_numpy(Q).to(dev)
+                with R.RMQIndex(dA, bs) as ix:
+                    fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+                    ms = time_steps(fn, max(3, args.steps // 2), 2, stream, barrier)
+                ref_nb[name] = {"nb": nb, "bs": bs, "rmq_s": job_rate(q, world, ms), "ms_per_step": ms}
+                del dQ
         del dA
         torch.cuda.empty_cache()
         batched = None if args.skip_batched else bench_batched(args, dev, stream, barrier)
@@ -624,6 +638,7 @@ def main():
         "random_access_roofline": h.get("random_access"),
         "clocks": clocks,
         "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
+        "modes_reference_nb": ref_nb,
         "energy": h.get("energy"),
         "batched": batched,
         "autograd": autograd,
