@@ -586,3 +586,50 @@ def test_cli_csv_nb_and_power(native, tmp_path):
         assert abs(qps * nsq / 1e9 - 1.0) < 1e-3   # q/s and ns/q are reciprocal
     if pw.exists():
         assert pw.stat().st_size > 0
+
+
+def test_abi_argument_errors(cuda, native):
+    """Every entry point rejects bad arguments with RMQ_EINVAL and a message,
+    without launching anything: NULL pointers, sizes out of range, misaligned
+    query / output buffers, NULL handles, malformed batch layouts."""
+    import ctypes as C
+
+    import torch
+
+    from rtxrmq_gb300._native import RMQ_EINVAL
+    L = native
+    A = torch.rand(1000, device=cuda)
+    Q = torch.zeros((10, 2), dtype=torch.int32, device=cuda)
+    out = torch.empty(16, dtype=torch.int32, device=cuda)
+    h = C.c_void_p()
+
+    def einval(rc):
+        assert rc == RMQ_EINVAL, rc
+        assert L.rmq_last_error_string()
+
+    einval(L.rmq_build(None, 1000, 64, None, C.byref(h)))
+    einval(L.rmq_build(A.data_ptr(), 0, 64, None, C.byref(h)))
+    einval(L.rmq_build(A.data_ptr(), 2**31, 64, None, C.byref(h)))
+    einval(L.rmq_build(A.data_ptr(), 1000, 64, None, None))
+    assert L.rmq_build(A.data_ptr(), 1000, 64, None, C.byref(h)) == 0
+    try:
+        einval(L.rmq_query(None, Q.data_ptr(), 10, None, out.data_ptr(), None))
+        einval(L.rmq_query(h, Q.data_ptr(), -1, None, out.data_ptr(), None))
+        einval(L.rmq_query(h, None, 10, None, out.data_ptr(), None))
+        einval(L.rmq_query(h, Q.data_ptr() + 4, 10, None, out.data_ptr(), None))   # 8-byte queries
+        einval(L.rmq_query(h, Q.data_ptr(), 10, None, None, None))                  # no output
+        einval(L.rmq_query(h, Q.data_ptr(), 10, None, out.data_ptr() + 2, None))   # misaligned output
+        einval(L.rmq_query_host(h, None, 10, None, out.data_ptr(), None))
+        einval(L.rmq_probe_gather(h, Q.data_ptr() + 4, 10, None, out.data_ptr(), None))
+        einval(L.rmq_info(h, None))
+    finally:
+        assert L.rmq_free(h) == 0
+    einval(L.rmq_query_scan(A.data_ptr(), 0, Q.data_ptr(), 10, None, out.data_ptr(), None))
+    b = C.c_void_p()
+    i64 = lambda *v: (C.c_int64 * len(v))(*v)  # noqa: E731
+    einval(L.rmq_batch_create(0, i64(0), i64(1), i64(0), i64(1), None, C.byref(b)))
+    einval(L.rmq_batch_create(1, i64(0), i64(-5), i64(0), i64(1), None, C.byref(b)))
+    einval(L.rmq_batch_create(1, i64(-1), i64(5), i64(0), i64(1), None, C.byref(b)))
+    einval(L.rmq_batch_create(1, None, i64(5), i64(0), i64(1), None, C.byref(b)))
+    einval(L.rmq_batch_run(None, A.data_ptr(), Q.data_ptr(), None, out.data_ptr(), None))
+    einval(L.rmq_batch_scatter_grad(None, out.data_ptr(), A.data_ptr(), A.data_ptr(), 0, None))
