@@ -71,15 +71,21 @@ void poll() {
 
 }  // namespace
 
+namespace rmq {
+int set_error(int code, const char *fmt, ...);  // api.cu: status + message for rmq_last_error_string
+}
+using rmq::set_error;
+
 extern "C" {
 
 int rmq_power_begin(int32_t device, int32_t sample_ms, int32_t cooldown_ms, const char *path) {
     std::lock_guard<std::mutex> lock(g_s.mu);
-    if (g_s.running) return RMQ_EINVAL;
-    if (sample_ms <= 0 || cooldown_ms < 0) return RMQ_EINVAL;
+    if (g_s.running) return set_error(RMQ_EINVAL, "rmq_power_begin: a sampling is already running");
+    if (sample_ms <= 0 || cooldown_ms < 0)
+        return set_error(RMQ_EINVAL, "rmq_power_begin: sample_ms must be > 0 and cooldown_ms >= 0");
     const char *name = std::getenv("RTXRMQ_NVML_LIBRARY");
     void *lib = dlopen(name && *name ? name : "libnvidia-ml.so.1", RTLD_NOW | RTLD_LOCAL);
-    if (!lib) return RMQ_ENOTSUP;
+    if (!lib) return set_error(RMQ_ENOTSUP, "rmq_power_begin: NVML library not found");
     auto init = reinterpret_cast<nvml_init_t>(dlsym(lib, "nvmlInit_v2"));
     auto shut = reinterpret_cast<nvml_shutdown_t>(dlsym(lib, "nvmlShutdown"));
     auto by_idx = reinterpret_cast<nvml_by_index_t>(dlsym(lib, "nvmlDeviceGetHandleByIndex_v2"));
@@ -87,7 +93,7 @@ int rmq_power_begin(int32_t device, int32_t sample_ms, int32_t cooldown_ms, cons
     auto pw = reinterpret_cast<nvml_power_t>(dlsym(lib, "nvmlDeviceGetPowerUsage"));
     if (!init || !shut || !by_idx || !pw || init() != 0) {
         dlclose(lib);
-        return RMQ_ENOTSUP;
+        return set_error(RMQ_ENOTSUP, "rmq_power_begin: NVML symbols missing or initialisation failed");
     }
     void *dev = nullptr;
     char bus[64];
@@ -99,7 +105,7 @@ int rmq_power_begin(int32_t device, int32_t sample_ms, int32_t cooldown_ms, cons
     if (!found && by_idx(static_cast<unsigned>(device), &dev) != 0) {
         shut();
         dlclose(lib);
-        return RMQ_ENOTSUP;
+        return set_error(RMQ_ENOTSUP, "rmq_power_begin: no NVML device for CUDA device %d", device);
     }
     FILE *fp = nullptr;
     if (path && *path) {
@@ -107,7 +113,7 @@ int rmq_power_begin(int32_t device, int32_t sample_ms, int32_t cooldown_ms, cons
         if (!fp) {
             shut();
             dlclose(lib);
-            return RMQ_EINVAL;
+            return set_error(RMQ_EINVAL, "rmq_power_begin: cannot open %s", path);
         }
         std::fprintf(fp, "%-15s %-15s %-15s %-15s %-15s %-15s\n", "#timestep", "power",
                      "acc-energy", "avg-power", "dt", "acc-time");
@@ -130,10 +136,12 @@ int rmq_power_end(int32_t cooldown_ms, double *avg_watts, double *energy_joules,
                   double *seconds) {
     {
         std::lock_guard<std::mutex> lock(g_s.mu);
-        if (!g_s.running) return RMQ_EINVAL;
+        if (!g_s.running) return set_error(RMQ_EINVAL, "rmq_power_end: no sampling is running");
     }
     if (cooldown_ms > 0) std::this_thread::sleep_for(std::chrono::milliseconds(cooldown_ms));
     std::lock_guard<std::mutex> lock(g_s.mu);
+    // another caller may have ended the sampling during the cool-down
+    if (!g_s.running) return set_error(RMQ_EINVAL, "rmq_power_end: no sampling is running");
     g_s.stop.store(true);
     g_s.th.join();
     if (g_s.fp) std::fclose(g_s.fp);
