@@ -548,17 +548,17 @@ def main():
                                                "how": "the step's query bytes in and result bytes out "
                                                       "copied concurrently (pinned, two streams)"}}
                 del hQ, hV, hI
+            # random-access ceiling on this index and this mode's queries:
+            # rmq_probe_gather has the query kernel's grid, query stream and
+            # stores but only two random lookups (suf[l], pre[r]) per query
+            gfn = lambda: ix.probe_gather(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+            gms = time_steps(gfn, args.steps, args.warmup, stream, barrier)
+            res["random_access"] = {
+                "ceiling_rmq_s": job_rate(q, world, gms), "ceiling_ms_per_step": gms,
+                "frac": gms / ms, "kernel": "gather_kernel (rmq_probe_gather)",
+                "pattern": "per query: 8-B query read, two random 8-B lookups (suf[l], pre[r]) "
+                           "in the 0.8 GB prefix / suffix tables, 8-B result write"}
             if lr == -1:
-                # random-access ceiling on this index: rmq_probe_gather has the
-                # query kernel's grid, query stream and stores but only its two
-                # random lookups (suf[l], pre[r]) per query
-                gfn = lambda: ix.probe_gather(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
-                gms = time_steps(gfn, args.steps, args.warmup, stream, barrier)
-                res["random_access"] = {
-                    "ceiling_rmq_s": job_rate(q, world, gms), "ceiling_ms_per_step": gms,
-                    "frac": gms / ms, "kernel": "gather_kernel (rmq_probe_gather)",
-                    "pattern": "per query: 8-B query read, two random 8-B lookups (suf[l], pre[r]) "
-                               "in the 0.8 GB prefix / suffix tables, 8-B result write"}
                 headline = (name, lr, Q, bs)
                 # energy: NVML board power over ~1.5 s of headline steps (outside
                 # the timed region), as the reference's power CSVs
@@ -636,6 +636,8 @@ def main():
                      "peak_kind": f"{peak_kind} copy bandwidth",
                      "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
         "random_access_roofline": h.get("random_access"),
+        "random_access_frac_by_mode": {k: v["random_access"]["frac"] for k, v in results.items()
+                                       if "random_access" in v},
         "clocks": clocks,
         "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
         "modes_reference_nb": ref_nb,
