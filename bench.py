@@ -6,7 +6,10 @@ q = 2^26 inclusive (l, r) queries, values and leftmost indices both returned.
 The headline step is one rmq_query over the uniform-length queries (lr=-1);
 the other length modes of the same configuration (lr=-2, lr=-3, fixed
 len 2^10) are timed the same way and reported under "modes". The block size
-of each mode is the fastest of a sweep over 2^10..2^16.
+of each mode is the fastest of a sweep over 2^10..2^16 (the workload's range)
+and 2^7..2^9 (short ranges are cheapest as cross-block queries over small
+blocks, whose coarse table stays in L2); "best_in_2^10..2^16" keeps the
+fastest inside the workload's range.
 
 value      -- RMQ/s of the device-resident step (inputs already in HBM),
               timed with CUDA events on the launching stream.
@@ -44,7 +47,7 @@ N_ELEMS = 10**8
 N_QUERIES = 1 << 26
 SEED = 1321
 MODES = [("lr=-1", -1), ("lr=-2", -2), ("lr=-3", -3), ("len=2^10", 1024)]
-BS_SWEEP = [1 << 10, 1 << 12, 1 << 14, 1 << 16]
+BS_SWEEP = [1 << 7, 1 << 8, 1 << 9, 1 << 10, 1 << 12, 1 << 14, 1 << 16]
 PUBLISHED_LR1 = 3.52e8  # RTXRMQ alg 5, RTX 6000 Ada (csv-to-plot/perf-RTX6000ADA-ALG5.csv:1586-1601)
 
 
@@ -153,7 +156,7 @@ def algorithmic_bytes(Q: np.ndarray, n: int, bs: int, out_bytes: int) -> tuple[f
 
     per_q = 8 + out_bytes
     total = per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge.sum()
-    micro = bs % 32 == 0 and bs >= 64
+    micro = bs >= 64  # the sub-block level exists for every bs >= 64
     if micro:
         # sub-block level: inside one 32-element micro-block a scan of its
         # line; otherwise one sector each for the in-micro-block suffix at l
@@ -495,6 +498,8 @@ def main():
             res = {"value": job_rate(q, world, ms), "ms_per_step": ms,
                    "ms_per_step_min": STEP_MIN[id(fn)], "bs": bs,
                    "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
+                   "best_in_2^10..2^16": max(((k, v) for k, v in sweep.items() if k >= 1 << 10),
+                                             key=lambda kv: kv[1], default=None),
                    "construction_ms": construction_ms, "mix": mix,
                    "alg_bytes_per_step": alg_bytes,
                    "achieved_gbs": alg_bytes / (ms / 1e3) / 1e9,
