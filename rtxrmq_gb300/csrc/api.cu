@@ -477,7 +477,10 @@ int rmq_info(const rmq_handle_t *h, rmq_info_t *info) {
     info->micro_levels = static_cast<int32_t>(h->plan.mlevels);
     info->reserved = 0;
     info->micro_table_bytes =
-        static_cast<int64_t>(sizeof(Entry) * static_cast<size_t>(h->plan.nmicro) * h->plan.mlevels);
+        h->plan.micro ? static_cast<int64_t>(static_cast<size_t>(h->plan.nmicro) *
+                                             (sizeof(Entry) + static_cast<size_t>(h->plan.moff_bytes) *
+                                                                  (h->plan.mlevels - 1)))
+                      : 0;
     info->is_max = (h->plan.kmode & 1u) ? 1 : 0;
     info->is_int32 = (h->plan.kmode >= kIntMin) ? 1 : 0;
     return RMQ_OK;

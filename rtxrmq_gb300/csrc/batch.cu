@@ -87,6 +87,8 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     v.suf = P.ws + a.pre + a.n;
     v.st = P.ws + a.st;
     v.mst = nullptr;  // batched arrays answer same-block queries with warp scans
+    v.moff = nullptr;
+    v.moff_bytes = 0u;
     v.nmicro = 0;
     v.mpre = nullptr;
     v.msuf = nullptr;
@@ -453,6 +455,8 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
         p.nmicro = 0;
         p.mlevels = 0;
         p.mst = nullptr;
+        p.moff = nullptr;
+        p.moff_bytes = 0u;
         p.mpre = nullptr;
         p.msuf = nullptr;
         p.kmode = kFloatMin;

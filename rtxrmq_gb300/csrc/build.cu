@@ -48,6 +48,30 @@ __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
         if (rmq_chk(j + half < nb)) cur[j] = better(prev[j], prev[j + half]);
 }
 
+// Level k >= 1 of the micro table as offsets: the window of 2^k micro-blocks
+// at i is the windows of 2^(k-1) at i and at i + 2^(k-1); each half's best
+// micro-block is found through the level below (level 0 = the minima
+// themselves), the better of the two kept as its offset from i. Unsigned
+// comparison of composites keeps the leftmost of equal minima.
+template <class O>
+__global__ void micro_level_kernel(const Entry *__restrict__ mst0, O *off, uint32_t nmicro,
+                                   uint32_t k) {
+    const uint32_t half = 1u << (k - 1);
+    const uint32_t cnt = nmicro - (1u << k) + 1;
+    O *cur = off + static_cast<size_t>(k - 1) * nmicro;
+    const O *prev = off + static_cast<size_t>(k >= 2 ? k - 2 : 0) * nmicro;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
+         i += gridDim.x * blockDim.x) {
+        uint32_t a = i, b = i + half;
+        if (k >= 2) {
+            a += prev[i];
+            b += prev[i + half];
+        }
+        if (rmq_chk(a < nmicro && b < nmicro && a - i < half && b - i < 2 * half))
+            cur[i] = static_cast<O>((mst0[b] < mst0[a] ? b : a) - i);
+    }
+}
+
 // Sub-block level: 8 lanes per 32-element micro-block, 4 consecutive
 // elements per lane (one 16-byte load), 4 micro-blocks per warp. Each lane
 // scans its 4 elements both ways, then the 8 lanes of a micro-block scan
@@ -137,6 +161,28 @@ cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceI
     return cudaSuccess;
 }
 
+template <class O>
+cudaError_t launch_micro_levels_w(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {
+    for (uint32_t k = 1; k < p.mlevels; ++k) {
+        const uint32_t cnt = p.nmicro - (1u << k) + 1;
+        uint32_t g = (cnt + 255) / 256;
+        const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
+        if (g > cap) g = cap;
+        micro_level_kernel<O><<<g, 256, 0, s>>>(p.mst, static_cast<O *>(p.moff), p.nmicro, k);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_micro_levels(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {
+    switch (p.moff_bytes) {
+    case 1: return launch_micro_levels_w<uint8_t>(p, dev, s);
+    case 2: return launch_micro_levels_w<uint16_t>(p, dev, s);
+    default: return launch_micro_levels_w<uint32_t>(p, dev, s);
+    }
+}
+
 }  // namespace
 
 uint32_t st_levels(uint32_t nb) { return nb ? static_cast<uint32_t>(ilog2(nb)) + 1u : 0u; }
@@ -144,7 +190,7 @@ uint32_t st_levels(uint32_t nb) { return nb ? static_cast<uint32_t>(ilog2(nb)) +
 namespace {
 size_t a256(size_t x) { return (x + 255) / 256 * 256; }
 struct Offsets {
-    size_t pre, suf, st, mst, mpre, msuf, counter, total;
+    size_t pre, suf, st, mst, moff, mpre, msuf, counter, total;
 };
 Offsets offsets_of(const BuildPlan &p) {
     Offsets o;
@@ -153,7 +199,9 @@ Offsets offsets_of(const BuildPlan &p) {
     o.suf = nent;
     o.st = 2 * nent;
     o.mst = o.st + a256(sizeof(Entry) * static_cast<size_t>(p.nb) * p.levels);
-    o.mpre = o.mst + a256(sizeof(Entry) * static_cast<size_t>(p.nmicro) * p.mlevels);
+    o.moff = o.mst + (p.micro ? a256(sizeof(Entry) * static_cast<size_t>(p.nmicro)) : 0);
+    o.mpre = o.moff + (p.micro ? a256(static_cast<size_t>(p.moff_bytes) * p.nmicro *
+                                      (p.mlevels - 1)) : 0);
     o.msuf = o.mpre + (p.micro ? nent : 0);
     o.counter = o.msuf + (p.micro ? nent : 0);
     o.total = o.counter + 256;
@@ -167,6 +215,7 @@ size_t plan_index(BuildPlan &p, bool no_micro) {
     p.mlevels = no_micro ? 0u : micro_levels(p.bs);
     p.micro = p.mlevels > 0;
     p.nmicro = p.micro ? (p.n + kMicro - 1) / kMicro : 0u;
+    p.moff_bytes = p.micro ? micro_offset_bytes(p.mlevels) : 0u;
     p.aligned = reinterpret_cast<uintptr_t>(p.A) % 16 == 0;
     return offsets_of(p).total;
 }
@@ -178,6 +227,7 @@ unsigned long long *place_index(BuildPlan &p, void *base_v) {
     p.suf = reinterpret_cast<Entry *>(base + o.suf);
     p.st = reinterpret_cast<Entry *>(base + o.st);
     p.mst = p.micro ? reinterpret_cast<Entry *>(base + o.mst) : nullptr;
+    p.moff = p.micro ? static_cast<void *>(base + o.moff) : nullptr;
     p.mpre = p.micro ? reinterpret_cast<Entry *>(base + o.mpre) : nullptr;
     p.msuf = p.micro ? reinterpret_cast<Entry *>(base + o.msuf) : nullptr;
     return reinterpret_cast<unsigned long long *>(base + o.counter);
@@ -241,7 +291,7 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
                                         p.aligned);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    return launch_levels(p.mst, p.nmicro, p.mlevels, dev, s);
+    return launch_micro_levels(p, dev, s);
 }
 
 RMQ_VIOLATIONS_READER(violations_build)

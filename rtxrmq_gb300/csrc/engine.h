@@ -81,13 +81,19 @@ struct BuildPlan {
     Entry *pre;   // [n]
     Entry *suf;   // [n]
     Entry *st;    // [levels * nb], level 0 = block minima
-    // sub-block level (only when bs is a multiple of kMicro): minima of the
-    // 32-element micro-blocks and a sparse table over them truncated to the
-    // window lengths a same-block query can need
+    // sub-block level (every bs >= 64): minima of the 32-element
+    // micro-blocks and a sparse table over them truncated to the window
+    // lengths a same-block query can need. Level 0 holds the micro-block
+    // minima as entries; level k >= 1 holds, for the window of 2^k
+    // micro-blocks starting at j, the offset (< 2^k) of its leftmost best
+    // micro-block in moff_bytes = 1, 2 or 4 bytes: 1/8 to 1/2 of the bytes
+    // of entries, so that the table stays in L2
     bool micro;
     uint32_t nmicro;   // ceil(n / 32)
     uint32_t mlevels;
-    Entry *mst;        // [mlevels * nmicro]
+    Entry *mst;        // [nmicro] micro-block minima (table level 0)
+    void *moff;        // [(mlevels - 1) * nmicro] offsets of levels 1 ..
+    uint32_t moff_bytes;
     Entry *mpre;       // [n] leftmost minimum of A[microstart(i) .. i]
     Entry *msuf;       // [n] leftmost minimum of A[i .. microend(i)]
     uint32_t kmode;    // KeyMode: float32 / int32 elements, minimum / maximum
@@ -95,6 +101,11 @@ struct BuildPlan {
 constexpr uint32_t kMicro = 32;
 // levels of the micro table for block size bs (0 when not applicable)
 uint32_t micro_levels(uint32_t bs);
+// bytes of one micro-table offset for a table of `mlevels` levels: the
+// largest offset is 2^(mlevels - 1) - 1
+inline uint32_t micro_offset_bytes(uint32_t mlevels) {
+    return mlevels <= 9 ? 1u : (mlevels <= 17 ? 2u : 4u);
+}
 
 // Fill the size fields of a plan (A, n, bs given; micro level on unless
 // `no_micro`); returns the bytes of the single allocation holding the index

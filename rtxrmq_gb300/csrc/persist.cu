@@ -19,7 +19,9 @@ namespace rmq {
 namespace {
 
 constexpr char kMagic[16] = "RTXRMQ-GB300-IX";
-constexpr uint32_t kVersion = 3;  // 2: entries are comparison composites; 3: sub-block level for every bs >= 64
+// 2: entries are comparison composites; 3: sub-block level for every
+// bs >= 64; 4: micro-table levels 1.. stored as offsets
+constexpr uint32_t kVersion = 4;
 constexpr size_t kIoChunk = size_t(64) << 20;
 
 struct FileHeader {

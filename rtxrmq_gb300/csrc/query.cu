@@ -127,6 +127,8 @@ V1View view_of(const BuildPlan &p) {
     v.suf = p.suf;
     v.st = p.st;
     v.mst = p.micro ? p.mst : nullptr;
+    v.moff = p.micro ? p.moff : nullptr;
+    v.moff_bytes = p.micro ? p.moff_bytes : 0u;
     v.nmicro = p.micro ? p.nmicro : 0u;
     v.mpre = p.micro ? p.mpre : nullptr;
     v.msuf = p.micro ? p.msuf : nullptr;

@@ -46,13 +46,15 @@ struct V1View {
     // sub-block level: 32-element micro-blocks (local index / 32), whatever
     // the block size; null when the index has none (same-block queries then
     // use the warp-cooperative scan)
-    const Entry *mst;
+    const Entry *mst;   // micro-block minima (micro-table level 0)
+    const void *moff;   // levels 1..: offsets of each window's best micro-block
+    uint32_t moff_bytes;
     uint32_t nmicro;
     const Entry *mpre;  // in-micro-block prefix / suffix minima
     const Entry *msuf;
     uint32_t kmode;     // KeyMode: element type and minimum / maximum
     uint32_t levels;    // sparse-table levels (st holds levels * nb entries)
-    uint32_t mlevels;   // micro-table levels (mst holds mlevels * nmicro entries)
+    uint32_t mlevels;   // micro-table levels (moff holds mlevels - 1 rows of nmicro)
 };
 
 // Range-checked accesses (rmq_chk, common.cuh): element loads by absolute
@@ -65,6 +67,23 @@ __device__ __forceinline__ uint4 ld_elem4(const V1View &v, int64_t g) {
 }
 __device__ __forceinline__ Entry ld_entry(const Entry *t, uint64_t i, uint64_t size) {
     return rmq_chk(i < size) ? t[i] : kEntryNone;
+}
+
+// The same, as a streaming load (evict-first in L1 and L2), for the random
+// per-element sub-block entries: they are read once, and the micro table
+// they would otherwise evict is read by every same-block query.
+__device__ __forceinline__ Entry ld_entry_cs(const Entry *t, uint64_t i, uint64_t size) {
+    return rmq_chk(i < size) ? __ldcs(reinterpret_cast<const unsigned long long *>(t) + i)
+                             : kEntryNone;
+}
+
+// Offset i of the micro table's levels 1.. (moff_bytes wide, the same for
+// every query of an index, so the branch does not diverge).
+__device__ __forceinline__ uint32_t ld_moff(const V1View &v, uint64_t i) {
+    if (!rmq_chk(i < static_cast<uint64_t>(v.mlevels - 1u) * v.nmicro)) return 0u;
+    if (v.moff_bytes == 1u) return static_cast<const uint8_t *>(v.moff)[i];
+    if (v.moff_bytes == 2u) return static_cast<const uint16_t *>(v.moff)[i];
+    return static_cast<const uint32_t *>(v.moff)[i];
 }
 
 // Leftmost minimum of local A[a..b] (b - a < 32, at most 9 16-byte loads)
@@ -108,20 +127,24 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
 
 // Same-block query through the sub-block level: the partial micro-blocks at
 // both ends from the in-micro-block suffix / prefix minima, the micro-blocks
-// between from the micro table; a query inside one micro-block is one
-// thread's scan of at most 32 values (one 128-byte line).
+// between from the micro table (two offsets, then the two micro-block minima
+// they point at; all of it L2-resident); a query inside one micro-block is
+// one thread's scan of at most 32 values (one 128-byte line).
 template <bool ALIGNED>
 __device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
     const uint32_t ml = l >> 5, mr = r >> 5;
     if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
-    Entry e = better(ld_entry(v.msuf, l, v.n), ld_entry(v.mpre, r, v.n));
+    Entry e = better(ld_entry_cs(v.msuf, l, v.n), ld_entry_cs(v.mpre, r, v.n));
     if (mr - ml >= 2u) {
         const uint32_t lo = ml + 1u, hi = mr - 1u;
         const int k = ilog2(hi - lo + 1u);
-        const uint64_t row = static_cast<uint64_t>(k) * v.nmicro;
-        const uint64_t size = static_cast<uint64_t>(v.mlevels) * v.nmicro;
-        e = better(e, better(ld_entry(v.mst, row + lo, size),
-                             ld_entry(v.mst, row + hi + 1u - (1u << k), size)));
+        uint32_t a = lo, b = hi + 1u - (1u << k);
+        if (k > 0) {
+            const uint64_t row = static_cast<uint64_t>(k - 1) * v.nmicro;
+            a += ld_moff(v, row + a);
+            b += ld_moff(v, row + b);
+        }
+        e = better(e, better(ld_entry(v.mst, a, v.nmicro), ld_entry(v.mst, b, v.nmicro)));
     }
     return e;
 }
