@@ -619,16 +619,21 @@ def main():
         return
     name, lr, Q, bs = headline if headline else (modes[0][0], modes[0][1], None, None)
     h = results[name]
+    bs = h["bs"]
     achieved = h["achieved_gbs"]
+    # the headline workload, or (a run of other modes / sizes) the one measured
+    default_run = lr == -1 and n == N_ELEMS and q == N_QUERIES
+    label = "n=1e8 q=2^26 lr=-1" if default_run else f"n={n} q={q} {name}"
     line = {
-        "metric": "RMQ/s n=1e8 q=2^26 lr=-1 (values+indices)",
+        "metric": f"RMQ/s {label} (values+indices)",
         "value": h["value"], "unit": "RMQ/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": h["ms_per_step"],
         "ms_per_step_min": h["ms_per_step_min"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": h["value"] / PUBLISHED_LR1,
         "vs_baseline_ref": "RTXRMQ (alg 5) on RTX 6000 Ada, 3.52e8 RMQ/s, n=1e8 q=2^26 lr=-1",
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices",
+        "config": {"workload": ("plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices"
+                                if default_run else f"plain RMQ {label}, values+indices"),
                    "n": n, "q": q, "lr": lr, "bs": bs, "seed": SEED,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "no flush: per-step working set (2.9 GB: values, pre/suf, queries, "
@@ -636,8 +641,10 @@ def main():
         "e2e": h.get("e2e"),
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": profiled_traffic(q),
-                     "traffic_source": TRAFFIC_PROFILE.name,
+                     "frac": achieved / hbm_peak,
+                     # DRAM bytes captured by ncu on the headline workload only
+                     "traffic": profiled_traffic(q) if default_run else None,
+                     "traffic_source": TRAFFIC_PROFILE.name if default_run else None,
                      "peak_kind": f"{peak_kind} copy bandwidth",
                      "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
         "random_access_roofline": h.get("random_access"),
