@@ -101,6 +101,26 @@ def test_length_modes_medium(cuda, native, oracle_lib, lr, bs, micro):
     assert_matches(A, Q, v, i, ev, ei)
 
 
+@pytest.mark.parametrize("bs", [(1 << 22) + 5, 1 << 23])
+@pytest.mark.parametrize("ties", [False, True])
+def test_huge_blocks_wide_offsets(cuda, native, oracle_lib, bs, ties):
+    """Blocks of 2^22+ elements: the micro table has 18+ levels, so its
+    offsets are 4 bytes wide; queries inside one block span up to the whole
+    block (every table level), on tie-free and tie-heavy values."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = (1 << 24) + 12345
+    A = R.gen_values_int(n, 16, 5) if ties else R.gen_values_uniform(n, 5)
+    Q = np.concatenate([R.gen_queries(1 << 12, n, length, 9 + k)
+                        for k, length in enumerate((-2, 1 << 16, 1 << 20, (1 << 22) - 100))])
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), bs) as ix:
+        assert ix.info()["micro_levels"] >= 18
+    v, i = run_index(cuda, A, Q, bs)
+    ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
+    assert_matches(A, Q, v, i, ev, ei)
+
+
 @pytest.mark.parametrize("micro", [True, False])
 @pytest.mark.parametrize("length", [1, 32, 33, 1 << 10, 1 << 16, 1 << 20])
 def test_tie_heavy(cuda, native, oracle_lib, length, micro):
