@@ -59,7 +59,7 @@ typedef struct rmq_info {
     int64_t struct_bytes; /* all device memory owned by the handle      */
     int32_t micro_levels; /* levels of the sub-block table (0 = none)   */
     int32_t reserved;
-    int64_t micro_table_bytes;
+    int64_t micro_table_bytes; /* micro-block minima + table offsets     */
     int32_t is_max;       /* 1: range maximum (RMQ_BUILD_MAX)           */
     int32_t is_int32;     /* 1: int32 elements (RMQ_BUILD_INT32)        */
 } rmq_info_t;
@@ -95,10 +95,12 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
  * rmq_build with options. When bs >= 64 the index
  * also gets a sub-block level -- prefix and suffix minima inside 32-element
  * micro-blocks (16 more bytes per element) and a sparse table over the
- * micro-block minima, truncated to windows shorter than one block -- so
- * that a query inside one block reads two entries and at most two table
- * entries (one 128-byte line if it lies inside one micro-block) instead of
- * scanning A[l..r]. RMQ_BUILD_NO_MICRO leaves it out.
+ * micro-block minima, truncated to windows shorter than one block and
+ * stored as 1-4 byte offsets to each window's best micro-block (small
+ * enough to stay in L2) -- so that a query inside one block reads two
+ * entries and at most four table values (one 128-byte line if it lies
+ * inside one micro-block) instead of scanning A[l..r].
+ * RMQ_BUILD_NO_MICRO leaves it out.
  * rmq_build(...) is rmq_build_ex(..., 0, ...).
  */
 int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags,
