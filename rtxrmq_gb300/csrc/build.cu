@@ -163,7 +163,9 @@ cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceI
 
 template <class O>
 cudaError_t launch_micro_levels_w(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {
-    for (uint32_t k = 1; k < p.mlevels; ++k) {
+    // bs <= n keeps every window inside the array (2^k <= nmicro); the
+    // bound is checked here as well
+    for (uint32_t k = 1; k < p.mlevels && (1u << k) <= p.nmicro; ++k) {
         const uint32_t cnt = p.nmicro - (1u << k) + 1;
         uint32_t g = (cnt + 255) / 256;
         const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
