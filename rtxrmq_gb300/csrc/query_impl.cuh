@@ -125,30 +125,6 @@ __device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, u
     return best;
 }
 
-// Same-block query through the sub-block level: the partial micro-blocks at
-// both ends from the in-micro-block suffix / prefix minima, the micro-blocks
-// between from the micro table (two offsets, then the two micro-block minima
-// they point at; all of it L2-resident); a query inside one micro-block is
-// one thread's scan of at most 32 values (one 128-byte line).
-template <bool ALIGNED>
-__device__ __forceinline__ Entry micro_query(const V1View &v, uint32_t l, uint32_t r) {
-    const uint32_t ml = l >> 5, mr = r >> 5;
-    if (ml == mr) return thread_range_min<ALIGNED>(v, l, r);
-    Entry e = better(ld_entry_cs(v.msuf, l, v.n), ld_entry_cs(v.mpre, r, v.n));
-    if (mr - ml >= 2u) {
-        const uint32_t lo = ml + 1u, hi = mr - 1u;
-        const int k = ilog2(hi - lo + 1u);
-        uint32_t a = lo, b = hi + 1u - (1u << k);
-        if (k > 0) {
-            const uint64_t row = static_cast<uint64_t>(k - 1) * v.nmicro;
-            a += ld_moff(v, row + a);
-            b += ld_moff(v, row + b);
-        }
-        e = better(e, better(ld_entry(v.mst, a, v.nmicro), ld_entry(v.mst, b, v.nmicro)));
-    }
-    return e;
-}
-
 struct QueryOut {
     const int2 *Q;        // queries of this array (local l, r)
     float *val;           // outputs aligned with Q, may be null
@@ -279,12 +255,38 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                 ea[k] = ld_entry(v.st, row + lo, size);
                 eb[k] = ld_entry(v.st, row + hi + 1u - (1u << lev), size);
             }
+            if (v.mst && scan[k] && (l[k] >> 5) != (r[k] >> 5)) {
+                // same block through the sub-block level, issued here beside the
+                // other queries' lookups so that all of them are in flight at
+                // once: the partial micro-blocks at both ends from the
+                // in-micro-block suffix / prefix minima, the micro-blocks between
+                // from the micro table (two offsets, then the two minima they
+                // point at; L2-resident). Only a query inside one micro-block
+                // is left to scan.
+                const uint32_t ml = l[k] >> 5, mr = r[k] >> 5;
+                es[k] = ld_entry_cs(v.msuf, l[k], v.n);
+                ep[k] = ld_entry_cs(v.mpre, r[k], v.n);
+                if (mr - ml >= 2u) {
+                    const uint32_t lo = ml + 1u, hi = mr - 1u;
+                    const int lev = ilog2(hi - lo + 1u);
+                    uint32_t a = lo, b = hi + 1u - (1u << lev);
+                    if (lev > 0) {
+                        const uint64_t row = static_cast<uint64_t>(lev - 1) * v.nmicro;
+                        a += ld_moff(v, row + a);
+                        b += ld_moff(v, row + b);
+                    }
+                    ea[k] = ld_entry(v.mst, a, v.nmicro);
+                    eb[k] = ld_entry(v.mst, b, v.nmicro);
+                }
+                scan[k] = false;
+            }
         }
         if (v.mst) {
             // sub-block level: every query of the step is answered by its own
-            // thread, so each result is stored once and a warp's 128-byte output
-            // line is written by one instruction (partial-line writes cost
-            // extra transactions, most of all to host memory)
+            // thread (a query inside one micro-block scans that micro-block's
+            // line), so each result is stored once and a warp's 128-byte
+            // output line is written by one instruction (partial-line writes
+            // cost extra transactions, most of all to host memory)
 #pragma unroll
             for (int k = 0; k < QPT; ++k) {
                 if (!act[k]) continue;
@@ -293,7 +295,7 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                     put_invalid(o, i);
                     continue;
                 }
-                const Entry e = scan[k] ? micro_query<ALIGNED>(v, l[k], r[k])
+                const Entry e = scan[k] ? thread_range_min<ALIGNED>(v, l[k], r[k])
                                         : better(better(es[k], ep[k]), better(ea[k], eb[k]));
                 put_result(o, i, e, v.kmode);
             }
