@@ -35,10 +35,16 @@ struct rmq_handle {
     cudaEvent_t k_done[3];     // per staging slot: kernel finished
     cudaEvent_t c_done[3];     // per staging slot: results copied out
     cudaEvent_t ev_end;
+    // per staging slot: used by an earlier chunk (of this call or an earlier
+    // one, whatever stream it was on), so its next use waits for that
+    // chunk's kernel and copy-out
+    bool slot_used[3];
 };
 
 namespace {
 constexpr int kHostStreams = 3;
+static_assert(sizeof(rmq_handle::slot_used) / sizeof(bool) == kHostStreams,
+              "one slot flag per staging slot");
 constexpr int64_t kHostChunk = int64_t(1) << 22;  // queries per staged chunk (64 MB of staging)
 }  // namespace
 
@@ -298,6 +304,7 @@ static cudaError_t release_staging(rmq_handle_t *h) {
             cudaEventDestroy(*e);
             *e = nullptr;
         }
+    for (bool &u : h->slot_used) u = false;
     cudaError_t err = cudaSuccess;
     if (h->stage) err = cudaFree(h->stage);
     h->stage = nullptr;
@@ -403,7 +410,8 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
     // streams: query copies in (hs), the chunk kernels in order (ks), result
     // copies out (cs), each chunk's steps ordered by per-slot events; a slot
     // is reused only when the kernel has read its queries and the copy-out
-    // has read its results.
+    // has read its results, including a slot last used by an earlier call
+    // on another stream.
     for (int64_t c = 0, i = 0; c < q && err == cudaSuccess; c += kHostChunk, ++i) {
         const int b = static_cast<int>(i % kHostStreams);
         const int64_t m = q - c < kHostChunk ? q - c : kHostChunk;
@@ -413,7 +421,7 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
             a.Q = qdev + c;
         } else {
             int32_t *dq = reinterpret_cast<int32_t *>(base);
-            if (i >= kHostStreams) err = cudaStreamWaitEvent(hm->hs, hm->k_done[b], 0);
+            if (hm->slot_used[b]) err = cudaStreamWaitEvent(hm->hs, hm->k_done[b], 0);
             if (err == cudaSuccess)
                 err = cudaMemcpyAsync(dq, h_queries + 2 * c, m * 8, cudaMemcpyHostToDevice, hm->hs);
             if (err == cudaSuccess) err = cudaEventRecord(hm->h_done[b], hm->hs);
@@ -421,7 +429,7 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
             if (err != cudaSuccess) break;
             a.Q = reinterpret_cast<const int2 *>(dq);
         }
-        if ((v_stage || i_stage) && i >= kHostStreams)
+        if ((v_stage || i_stage) && hm->slot_used[b])
             err = cudaStreamWaitEvent(hm->ks, hm->c_done[b], 0);
         if (err != cudaSuccess) break;
         float *dv = !h_val ? nullptr : v_stage ? reinterpret_cast<float *>(base + kHostChunk * 8) : vdev + c;
@@ -441,6 +449,7 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q, f
                 err = cudaMemcpyAsync(h_idx + c, di, m * 4, cudaMemcpyDeviceToHost, hm->cs);
             if (err == cudaSuccess) err = cudaEventRecord(hm->c_done[b], hm->cs);
         }
+        if (err == cudaSuccess) hm->slot_used[b] = true;
     }
     // `stream` continues when the kernel and copy-out streams are done (the
     // query copies precede their kernels)

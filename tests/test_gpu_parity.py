@@ -340,6 +340,38 @@ def test_query_host_staged_path(cuda, native, oracle_lib, monkeypatch):
             np.testing.assert_array_equal(bits(hv.numpy()), bits(dv))
 
 
+def test_query_host_staged_two_streams(cuda, native, oracle_lib, monkeypatch):
+    """Two staged host calls on one handle from two streams, enqueued back to
+    back: the second call's chunks reuse staging slots only after the first
+    call's kernels and copies are done with them."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    monkeypatch.setenv("RTXRMQ_HOST_STAGED", "1")
+    n = 1 << 21
+    A = R.gen_values_uniform(n, 41)
+    Q1 = R.gen_queries((1 << 24) + 5, n, -1, 41)   # five chunks
+    Q2 = R.gen_queries((1 << 22) + 3, n, -3, 42)   # two chunks
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), 4096) as ix:
+        want = []
+        for Q in (Q1, Q2):
+            dv, di = ix.query(torch.from_numpy(Q).to(cuda))
+            want.append((dv.cpu().numpy(), di.cpu().numpy()))
+        torch.cuda.synchronize()
+        outs = []
+        for Q, s in ((Q1, s1), (Q2, s2)):
+            hv = torch.empty(len(Q), dtype=torch.float32)
+            hi = torch.empty(len(Q), dtype=torch.int32)
+            ix.query_host(torch.from_numpy(Q), hv, hi, stream=s)
+            outs.append((hv, hi))
+        s1.synchronize()
+        s2.synchronize()
+        for (hv, hi), (dv, di) in zip(outs, want):
+            np.testing.assert_array_equal(hi.numpy(), di)
+            np.testing.assert_array_equal(bits(hv.numpy()), bits(dv))
+
+
 def test_save_load_index(cuda, native, oracle_lib, tmp_path):
     """rmq_save / rmq_load (the role of HRMQ's saveDS / loadDS): a loaded
     index answers like the built one; other values, lengths, foreign or
