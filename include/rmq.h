@@ -136,7 +136,10 @@ int rmq_query(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
  * and events on its first call on a handle, all or nothing.
  * Stream ordered with respect to `stream`: the results are in the host
  * buffers once `stream` has been synchronised. Calls on one handle from
- * several threads are serialised on the staged path. This is the end-to-end
+ * several threads or streams are safe: on the staged path their enqueueing
+ * is serialised and a staging slot is reused only after the kernel and the
+ * copies of its previous chunk, whichever call and stream that was on. This
+ * is the end-to-end
  * form of the reference's timed loop plus its copy-out (src/rtx.h:150-159).
  *
  * Environment switches read by the library:
