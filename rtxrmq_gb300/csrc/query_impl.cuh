@@ -77,13 +77,41 @@ __device__ __forceinline__ Entry ld_entry_cs(const Entry *t, uint64_t i, uint64_
                              : kEntryNone;
 }
 
+// The tables a query reads beside its two random per-element lookups (the
+// sparse table over block minima, the micro table) are small; their loads
+// carry an L2 evict-last policy (PTX createpolicy + ld.L2::cache_hint) so
+// that the per-element lines streaming through L2 evict them last. No L2
+// carve-out is set aside, unlike a persisting access-policy window. The
+// policy is made at each load: holding it across the step costs registers
+// (and resident CTAs) for nothing measurable.
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ Entry ld_entry_keep(const Entry *t, uint64_t i, uint64_t size,
+                                               uint64_t pol) {
+    if (!rmq_chk(i < size)) return kEntryNone;
+    unsigned long long v;
+    asm volatile("ld.global.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(t + i), "l"(pol));
+    return v;
+}
+
 // Offset i of the micro table's levels 1.. (moff_bytes wide, the same for
 // every query of an index, so the branch does not diverge).
-__device__ __forceinline__ uint32_t ld_moff(const V1View &v, uint64_t i) {
+__device__ __forceinline__ uint32_t ld_moff(const V1View &v, uint64_t i, uint64_t pol) {
     if (!rmq_chk(i < static_cast<uint64_t>(v.mlevels - 1u) * v.nmicro)) return 0u;
-    if (v.moff_bytes == 1u) return static_cast<const uint8_t *>(v.moff)[i];
-    if (v.moff_bytes == 2u) return static_cast<const uint16_t *>(v.moff)[i];
-    return static_cast<const uint32_t *>(v.moff)[i];
+    uint32_t r;
+    if (v.moff_bytes == 1u)
+        asm volatile("ld.global.L2::cache_hint.u8 %0, [%1], %2;"
+                     : "=r"(r) : "l"(static_cast<const uint8_t *>(v.moff) + i), "l"(pol));
+    else if (v.moff_bytes == 2u)
+        asm volatile("ld.global.L2::cache_hint.u16 %0, [%1], %2;"
+                     : "=r"(r) : "l"(static_cast<const uint16_t *>(v.moff) + i), "l"(pol));
+    else
+        asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;"
+                     : "=r"(r) : "l"(static_cast<const uint32_t *>(v.moff) + i), "l"(pol));
+    return r;
 }
 
 // Leftmost minimum of local A[a..b] (b - a < 32, at most 9 16-byte loads)
@@ -252,8 +280,8 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                 const int lev = ilog2(hi - lo + 1u);
                 const uint64_t row = static_cast<uint64_t>(lev) * v.nb;
                 const uint64_t size = static_cast<uint64_t>(v.levels) * v.nb;
-                ea[k] = ld_entry(v.st, row + lo, size);
-                eb[k] = ld_entry(v.st, row + hi + 1u - (1u << lev), size);
+                ea[k] = ld_entry_keep(v.st, row + lo, size, l2_keep_policy());
+                eb[k] = ld_entry_keep(v.st, row + hi + 1u - (1u << lev), size, l2_keep_policy());
             }
             if (v.mst && scan[k] && (l[k] >> 5) != (r[k] >> 5)) {
                 // same block through the sub-block level, issued here beside the
@@ -272,11 +300,11 @@ __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, 
                     uint32_t a = lo, b = hi + 1u - (1u << lev);
                     if (lev > 0) {
                         const uint64_t row = static_cast<uint64_t>(lev - 1) * v.nmicro;
-                        a += ld_moff(v, row + a);
-                        b += ld_moff(v, row + b);
+                        a += ld_moff(v, row + a, l2_keep_policy());
+                        b += ld_moff(v, row + b, l2_keep_policy());
                     }
-                    ea[k] = ld_entry(v.mst, a, v.nmicro);
-                    eb[k] = ld_entry(v.mst, b, v.nmicro);
+                    ea[k] = ld_entry_keep(v.mst, a, v.nmicro, l2_keep_policy());
+                    eb[k] = ld_entry_keep(v.mst, b, v.nmicro, l2_keep_policy());
                 }
                 scan[k] = false;
             }
