@@ -458,6 +458,62 @@ def test_key_modes(cuda, native, dtype, op, micro):
         np.testing.assert_array_equal(v.view(np.uint32), A[ei].view(np.uint32))
 
 
+def random_case(seed):
+    """One seeded random configuration: size, block size, element type, min /
+    max, sub-block level on / off, values pointer offset (unaligned for
+    offsets 1-3), value distribution and a mix of query lengths."""
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(1000 + seed)
+    edge_sizes = [1, 2, 31, 32, 33, 63, 64, 65, 95, 96, 97, 1000, 4095, 4096, 4097]
+    n = int(rng.choice(edge_sizes)) if rng.random() < 0.4 else int(rng.integers(1, 200_000))
+    if rng.random() < 0.5:
+        bs = int(rng.integers(1, n + 1))
+    else:
+        bs = min(n, int(rng.choice([1, 16, 32, 33, 64, 96, 1024, 4096, 65536])))
+    dtype = str(rng.choice(["float32", "int32"]))
+    op = str(rng.choice(["min", "max"]))
+    micro = bool(rng.random() < 0.7)
+    off = int(rng.integers(0, 4))
+    kind = int(rng.integers(0, 3))
+    if dtype == "float32":
+        A = (rng.random(n).astype(np.float32) if kind == 0 else
+             rng.integers(0, 8, n).astype(np.float32) if kind == 1 else
+             rng.standard_normal(n).astype(np.float32))
+        if kind == 2:
+            A[rng.integers(0, n, max(1, n // 50))] = -0.0
+    else:
+        A = (rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32) if kind == 0 else
+             rng.integers(-4, 4, n).astype(np.int32))
+    qs = [R.gen_queries(600, n, L, seed + k) for k, L in enumerate((-1, -2, -3))]
+    qs += [R.gen_queries(300, n, L, seed + 10 + k) for k, L in
+           enumerate((1, 2, 31, 32, 33, 64, 1000)) if L <= n]
+    qs.append(np.array([[0, n - 1], [n - 1, n - 1], [0, 0]], dtype=np.int32))
+    return n, bs, dtype, op, micro, off, A, np.concatenate(qs)
+
+
+@pytest.mark.parametrize("seed", range(64))
+def test_random_configurations(cuda, native, seed):
+    """Seeded random configurations (random_case) against a brute-force
+    leftmost argmin / argmax, values compared as bits."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n, bs, dtype, op, micro, off, A, Q = random_case(seed)
+    ei = np_leftmost(A, Q, op)
+    pad = np.zeros(off, dtype=A.dtype)
+    big = torch.from_numpy(np.concatenate([pad, A])).to(cuda)
+    dA = big[off:off + n]
+    with R.RMQIndex(dA, bs, micro=micro, op=op) as ix:
+        assert ix.info()["aligned"] == (1 if off == 0 else 0)
+        v, i = ix.query(torch.from_numpy(Q).to(cuda))
+        torch.cuda.synchronize()
+        i, v = i.cpu().numpy(), v.cpu().numpy()
+    cfg = f"n={n} bs={bs} {dtype} {op} micro={micro} off={off}"
+    bad = np.nonzero(i != ei)[0]
+    assert bad.size == 0, f"{cfg}: {bad.size} index mismatches, first {tuple(Q[bad[0]])}"
+    np.testing.assert_array_equal(v.view(np.uint32), A[ei].view(np.uint32), err_msg=cfg)
+
+
 def test_probe_gather(cuda, native, oracle_lib):
     """rmq_probe_gather (the random-access ceiling the bench times beside
     rmq_query) reads suf[l] and pre[r] only: exact for queries whose ends lie
