@@ -88,6 +88,60 @@ def test_batch_matches_oracle(cuda, native, oracle_lib, seed, ties, align, cfg):
     np.testing.assert_array_equal(bits(v2[own]), bits(ev[own]))
 
 
+def random_batch(seed):
+    """A seeded random batch: 1-300 arrays of lengths 0 .. 2^16 placed anywhere
+    in one values buffer (arrays may overlap: values are only read), query
+    sets of 0-200 queries with gaps between them, queries for empty arrays
+    (invalid by definition), and a random block size per size bucket."""
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(500 + seed)
+    k = int(rng.integers(1, 301))
+    pick = rng.random(k)
+    lengths = np.where(pick < 0.1, 0, np.where(pick < 0.4, rng.integers(1, 100, k),
+                                               np.round(2.0 ** rng.uniform(7, 16, k)))).astype(np.int64)
+    span = int(lengths.max()) + int(rng.integers(1, 200_000))
+    starts = np.array([rng.integers(0, span - n + 1) for n in lengths], np.int64)
+    A = (R.gen_values_int(span, 16, seed) if seed % 2 else R.gen_values_uniform(span, seed))
+    qcounts = rng.integers(0, 201, k).astype(np.int64)
+    qgap = rng.integers(0, 5, k)
+    qstarts = np.cumsum(np.concatenate([[qgap[0]], qcounts[:-1] + qgap[1:]])).astype(np.int64)
+    Q = np.zeros((int(qstarts[-1] + qcounts[-1] + 3), 2), dtype=np.int32)
+    for i, (n, c, q0) in enumerate(zip(lengths, qcounts, qstarts)):
+        if c and n:
+            L = [-1, -3, 1, 2, 33][i % 5]
+            Q[q0:q0 + c] = R.gen_queries(int(c), int(n), L if L < 0 or L <= n else -1, seed + i)
+    choices = [0, 1, 3, 16, 33, 64, 100, 256, 1024, 4096, 65536]
+    bucket_bs = [int(rng.choice(choices)) for _ in range(32)]
+    return starts, lengths, qstarts, qcounts, A, Q, bucket_bs
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_batch_random(cuda, native, oracle_lib, seed):
+    """random_batch: the batched launch and the per-array path against the
+    oracle per array; queries of empty arrays give -1 / NaN and are counted."""
+    import torch
+
+    from rtxrmq_gb300.batch import RMQBatch
+    starts, lengths, qstarts, qcounts, A, Q, bucket_bs = random_batch(seed)
+    live = lengths > 0
+    ev, ei = expected(oracle_lib, starts[live], lengths[live], qstarts[live], qcounts[live], A, Q)
+    own = owned_mask(qstarts[live], qcounts[live], len(Q))
+    dead = owned_mask(qstarts[~live], qcounts[~live], len(Q))
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    with RMQBatch(starts, lengths, qstarts, qcounts, bucket_bs) as b:
+        v, i = b.run(dA, dQ)
+        torch.cuda.synchronize()
+        v, i = v.cpu().numpy(), i.cpu().numpy()
+        assert b.invalid_count() == int(dead.sum())
+        v2, i2 = b.run_per_array(dA, dQ)
+        v2, i2 = v2.cpu().numpy(), i2.cpu().numpy()
+    for vv, ii in ((v, i), (v2, i2)):
+        np.testing.assert_array_equal(ii[own], ei[own])
+        np.testing.assert_array_equal(bits(vv[own]), bits(ev[own]))
+    assert (i[dead] == -1).all() and np.isnan(v[dead]).all()
+
+
 def test_batch_invalid_and_repeat(cuda, native, oracle_lib):
     """Invalid queries inside a batch give -1 / NaN and are counted; a plan
     runs repeatedly on new values without re-planning."""
