@@ -5,8 +5,9 @@ accessed. Every entry point is run through that build on the edge layouts
 (block sizes 1 .. 2^20 around the builder's one-tile / two-phase / streamed
 paths, unaligned values, invalid queries, key modes, host buffers in place
 and staged, save / load, the probe, the no-allocation entry, batches with
-odd offsets and empty arrays, the per-array path, the gradient scatter);
-the answers must equal the oracle's and no violation may be counted."""
+odd offsets and empty arrays, the per-array path, the gradient scatter, and
+the seeded random configurations and batches of the parity tests); the
+answers must equal the oracle's and no violation may be counted."""
 import json
 import subprocess
 import sys
@@ -124,6 +125,29 @@ for cfg in (None, [1] * 32, [64] * 32, [1000] * 32, [4096] * 32, [1 << 16] * 32)
         b.scatter_grad(i, torch.ones(len(Qb), device=dev), g)
         torch.cuda.synchronize()
         assert abs(float(g.sum()) - float(nonempty.sum())) < 0.5
+    ran += 1
+
+# the seeded random configurations of the parity tests
+sys.path.insert(0, "tests")
+import test_gpu_batch as TB
+import test_gpu_parity as TP
+for seed in range(64):
+    n, bs, dtype, op, micro, off, A, Q = TP.random_case(seed)
+    ei = TP.np_leftmost(A, Q, op)
+    big = torch.from_numpy(np.concatenate([np.zeros(off, dtype=A.dtype), A])).to(dev)
+    with R.RMQIndex(big[off:off + n], bs, micro=micro, op=op) as ix:
+        v, i = ix.query(torch.from_numpy(Q).to(dev))
+        eq(i.cpu().numpy(), ei, f"random case {seed}")
+        eq(v.cpu().numpy().view(np.uint32), A[ei].view(np.uint32), f"random case {seed} values")
+    ran += 1
+for seed in range(24):
+    starts, lengths, qstarts, qcounts, V, Qr, bucket_bs = TB.random_batch(seed)
+    live = lengths > 0
+    ev, ei = TB.expected(oracle, starts[live], lengths[live], qstarts[live], qcounts[live], V, Qr)
+    own = TB.owned_mask(qstarts[live], qcounts[live], len(Qr))
+    with RMQBatch(starts, lengths, qstarts, qcounts, bucket_bs) as b:
+        v, i = b.run(torch.from_numpy(V).to(dev), torch.from_numpy(Qr).to(dev))
+        eq(i.cpu().numpy()[own], ei[own], f"random batch {seed}")
     ran += 1
 
 cnt = C.c_int64()
