@@ -155,7 +155,10 @@ def algorithmic_bytes(Q: np.ndarray, n: int, bs: int, out_bytes: int) -> tuple[f
         return (b * 4) // 32 - (a * 4) // 32 + 1
 
     per_q = 8 + out_bytes
-    total = per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge.sum()
+    # an edge query loads suf[l] when r ends its block and pre[r] when l
+    # starts it (both for a query over one whole block)
+    edge_sec = ((~cross) & (r == bend)).sum() + ((~cross) & (l == bstart)).sum()
+    total = per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge_sec
     micro = bs >= 64  # the sub-block level exists for every bs >= 64
     if micro:
         # sub-block level: inside one 32-element micro-block a scan of its

@@ -279,3 +279,36 @@ def test_batch_argument_types(native):
         B._queries(torch.zeros((4, 2), dtype=torch.int64))
     with pytest.raises(TypeError):
         B._queries(torch.zeros((4, 3), dtype=torch.int32))
+
+
+def test_algorithmic_bytes_per_query(native):
+    """bench.py's algorithmic bytes equal a per-query count that follows the
+    query kernel's decisions one query at a time."""
+    import importlib.util
+
+    import rtxrmq_gb300 as R
+    spec = importlib.util.spec_from_file_location("bench", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    def one(l, r, n, bs):
+        b = 16  # query + value and index
+        lb, rb = l // bs, r // bs
+        if lb != rb:
+            return b + 64
+        bstart, bend = lb * bs, min(lb * bs + bs, n) - 1
+        if l == bstart or r == bend:
+            return b + 32 * ((r == bend) + (l == bstart))
+        if bs >= 64:
+            if l // 32 == r // 32:
+                return b + 32 * ((4 * r) // 32 - (4 * l) // 32 + 1)
+            return b + 64 + (64 if r // 32 - l // 32 >= 2 else 0)
+        return b + 32 * ((4 * r) // 32 - (4 * l) // 32 + 1)
+
+    n = 5000
+    Q = np.concatenate([R.gen_queries(700, n, L, 3 + k)
+                        for k, L in enumerate((-1, -2, -3, 1, 31, 64, 1000))])
+    Q = np.concatenate([Q, np.array([[0, 99], [100, 199], [0, n - 1], [4900, 4999]], np.int32)])
+    for bs in (1, 7, 32, 50, 64, 100, 1024, n):
+        total, _ = bench.algorithmic_bytes(Q, n, bs, 8)
+        assert total == sum(one(int(l), int(r), n, bs) for l, r in Q), bs
