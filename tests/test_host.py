@@ -312,3 +312,26 @@ def test_algorithmic_bytes_per_query(native):
     for bs in (1, 7, 32, 50, 64, 100, 1024, n):
         total, _ = bench.algorithmic_bytes(Q, n, bs, 8)
         assert total == sum(one(int(l), int(r), n, bs) for l, r in Q), bs
+
+
+def test_random_parity_cases_are_valid(native):
+    """The seeded random configurations of the GPU parity tests produce
+    in-range queries and consistent layouts (checked here without a GPU)."""
+    import sys
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    import test_gpu_batch as TB
+    import test_gpu_parity as TP
+    for seed in range(64):
+        n, bs, dtype, op, micro, off, A, Q = TP.random_case(seed)
+        assert 1 <= bs <= n and len(A) == n and 0 <= off < 4
+        assert A.dtype == np.dtype(dtype) and op in ("min", "max")
+        assert (Q[:, 0] >= 0).all() and (Q[:, 0] <= Q[:, 1]).all() and (Q[:, 1] < n).all()
+    for seed in range(24):
+        starts, lengths, qstarts, qcounts, V, Q, bucket_bs = TB.random_batch(seed)
+        assert (starts >= 0).all() and (starts + lengths <= len(V)).all() and len(bucket_bs) == 32
+        assert (qstarts[1:] >= qstarts[:-1] + qcounts[:-1]).all()
+        assert (qstarts + qcounts <= len(Q)).all()
+        for n, q0, c in zip(lengths, qstarts, qcounts):
+            if n and c:
+                q = Q[q0:q0 + c]
+                assert (q[:, 0] >= 0).all() and (q[:, 0] <= q[:, 1]).all() and (q[:, 1] < n).all()
