@@ -40,8 +40,10 @@ typedef struct CUstream_st *rmq_stream_t;
 #define RMQ_EINVAL   (-1)  /* bad argument (size, alignment, null pointer) */
 #define RMQ_ENOMEM   (-2)  /* device or host allocation failed            */
 #define RMQ_ECUDA    (-3)  /* a CUDA runtime call failed                  */
-#define RMQ_ETIMEOUT (-4)  /* a bounded device wait expired               */
 #define RMQ_ENOTSUP  (-5)  /* algorithm or mode not available             */
+/* (-4) is not used: no call of this library waits on the device with a
+ * time limit (the batched kernel's phase barriers are grid syncs of a
+ * cooperative launch, whose CTAs are all resident). */
 
 /* Default block size when bs <= 0: 2^15, as the reference CLI
  * (src/tools.h:96). */
@@ -95,11 +97,12 @@ int rmq_build(const float *d_vals, int64_t n, int64_t bs, rmq_stream_t stream,
  * rmq_build with options. When bs >= 64 the index
  * also gets a sub-block level -- prefix and suffix minima inside 32-element
  * micro-blocks (16 more bytes per element) and a sparse table over the
- * micro-block minima, truncated to windows shorter than one block and
+ * micro-block minima, truncated to windows no longer than one block and
  * stored as 1-4 byte offsets to each window's best micro-block (small
- * enough to stay in L2) -- so that a query inside one block reads two
- * entries and at most four table values (one 128-byte line if it lies
- * inside one micro-block) instead of scanning A[l..r].
+ * enough to stay in L2). A query spanning at most about two blocks is then
+ * answered from that table: usually from its table words alone, otherwise
+ * with one or two per-element entries (one 128-byte line of values if it
+ * lies inside one micro-block), never by scanning A[l..r].
  * RMQ_BUILD_NO_MICRO leaves it out.
  * rmq_build(...) is rmq_build_ex(..., 0, ...).
  */
@@ -233,6 +236,42 @@ int rmq_query_scan(const float *d_vals, int64_t n, const int32_t *d_queries,
  */
 int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
                      float *d_val, int32_t *d_idx, rmq_stream_t stream);
+
+/*
+ * Measurement helper, no reference counterpart: rmq_query (same arguments,
+ * same results; d_val and d_idx may both be NULL here) through an
+ * instantiation of the query kernel that also counts how every query was
+ * settled and what it read, into h_counts[RMQ_QUERY_STATS_FIELDS]:
+ *   [0] settled by the probe of the small table over every unit (block or
+ *       32-element micro-block) the query touches: the best of that
+ *       superset lay inside [l, r]
+ *   [1] settled by a narrower probe plus one per-element entry
+ *   [2] the three-part decomposition (two entries, probe of the middle)
+ *   [3] inside one micro-block: one thread scans it
+ *   [4] inside one block without the sub-block level: an edge entry
+ *   [5] inside one block without the sub-block level: warp scan
+ *   [6] per-element entries read (random 8-byte HBM lookups)
+ *   [7] small-table words read (L2-resident probes)
+ *   [8] 32-byte sectors of the values read by scans
+ *   [9] invalid queries
+ * Synchronises `stream`. Uses the handle's counter block, so concurrent
+ * rmq_query_stats calls on one handle race (rmq_query does not).
+ */
+#define RMQ_QUERY_STATS_FIELDS 10
+int rmq_query_stats(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
+                    float *d_val, int32_t *d_idx, int64_t *h_counts,
+                    rmq_stream_t stream);
+
+/*
+ * Measurement helper, no reference counterpart: the random-access rate of
+ * the GPU for this query stream, independent of any index layout. One
+ * launch with rmq_query's grid, query stream and output stores, and per
+ * query two 8-byte loads at positions hashed from (query number, l, r),
+ * uniform over d_buf[0 .. words). The outputs carry the loaded words, not
+ * range minima. Queries are read but not validated.
+ */
+int rmq_probe_random(const uint64_t *d_buf, int64_t words, const int32_t *d_queries,
+                     int64_t q, float *d_val, int32_t *d_idx, rmq_stream_t stream);
 
 /*
  * Checked builds only, no reference counterpart (the library compiled with

@@ -23,7 +23,7 @@ from ._native import LIB_PATH, RMQError, check, load, rmq_info_t
 __all__ = [
     "RMQIndex", "RMQError", "rtx_rmq", "gpu_rmq_basic", "gpu_rmq_basic_idx", "bs_from_nb",
     "gen_values_uniform", "gen_values_normal", "gen_values_int", "gen_queries",
-    "gen_queries_lognormal", "ALG_GPU_BASE", "ALG_GPU_RTX_BLOCKS", "ALG_GPU_BASE_IDX",
+    "gen_queries_lognormal", "probe_random", "ALG_GPU_BASE", "ALG_GPU_RTX_BLOCKS", "ALG_GPU_BASE_IDX",
     "ALG_GPU_RTX_BLOCKS_IDX", "DEFAULT_BS", "LIB_PATH", "load",
 ]
 
@@ -148,6 +148,20 @@ class RMQIndex:
                                       _stream_handle(stream)))
         return out_val, out_idx
 
+    STATS_FIELDS = ("first_probe", "second_probe", "full", "micro_scan", "block_edge",
+                    "warp_scan", "entries", "table_words", "scan_sectors", "invalid")
+
+    def query_stats(self, queries, out_val=None, out_idx=None, stream=None) -> dict:
+        """rmq_query_stats: the same answers as query() (into out_val /
+        out_idx when given) from the counting instantiation of the query
+        kernel, and how every query was settled and what it read (field
+        names in STATS_FIELDS). Synchronises the stream."""
+        q = _check_queries(queries)
+        counts = (C.c_int64 * len(self.STATS_FIELDS))()
+        check(load().rmq_query_stats(self._h, _dptr(queries), q, _dptr(out_val), _dptr(out_idx),
+                                     counts, _stream_handle(stream)))
+        return dict(zip(self.STATS_FIELDS, (int(x) for x in counts)))
+
     def save(self, path, stream=None) -> None:
         """Write the index (not the values) to ``path`` (rmq_save)."""
         check(load().rmq_save(self._h, str(path).encode(), _stream_handle(stream)))
@@ -192,6 +206,23 @@ class RMQIndex:
             self.close()
         except Exception:
             pass
+
+
+def probe_random(buf, queries, out_val=None, out_idx=None, stream=None) -> Tuple:
+    """rmq_probe_random: per query two random 8-byte loads from the int64
+    CUDA tensor ``buf`` with the query kernel's grid, query stream and
+    stores (the GPU's random-access rate, independent of any index)."""
+    import torch
+    q = _check_queries(queries)
+    if buf.dtype != torch.int64 or buf.dim() != 1:
+        raise TypeError("buf must be a 1-D int64 CUDA tensor")
+    if out_val is None:
+        out_val = torch.empty(q, dtype=torch.float32, device=queries.device)
+    if out_idx is None:
+        out_idx = torch.empty(q, dtype=torch.int32, device=queries.device)
+    check(load().rmq_probe_random(_dptr(buf), buf.numel(), _dptr(queries), q, _dptr(out_val),
+                                  _dptr(out_idx), _stream_handle(stream)))
+    return out_val, out_idx
 
 
 def bs_from_nb(n: int, nb: int) -> int:

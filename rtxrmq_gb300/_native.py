@@ -15,11 +15,10 @@ RMQ_OK = 0
 RMQ_EINVAL = -1
 RMQ_ENOMEM = -2
 RMQ_ECUDA = -3
-RMQ_ETIMEOUT = -4
 RMQ_ENOTSUP = -5
 
 _STATUS_NAMES = {RMQ_EINVAL: "RMQ_EINVAL", RMQ_ENOMEM: "RMQ_ENOMEM", RMQ_ECUDA: "RMQ_ECUDA",
-                 RMQ_ETIMEOUT: "RMQ_ETIMEOUT", RMQ_ENOTSUP: "RMQ_ENOTSUP"}
+                 RMQ_ENOTSUP: "RMQ_ENOTSUP"}
 
 
 class RMQError(RuntimeError):
@@ -70,6 +69,8 @@ SIGNATURES = {
     "rmq_bs_from_nb": (C.c_int, [_i64, _i64, C.POINTER(_i64)]),
     "rmq_query_scan": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_probe_gather": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "rmq_query_stats": (C.c_int, [_vp, _vp, _i64, _vp, _vp, C.POINTER(_i64), _vp]),
+    "rmq_probe_random": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_checked_violations": (C.c_int, [C.POINTER(_i64)]),
     "rmq_batch_create": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
     "rmq_batch_run": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),

@@ -46,6 +46,10 @@ constexpr int kHostStreams = 3;
 static_assert(sizeof(rmq_handle::slot_used) / sizeof(bool) == kHostStreams,
               "one slot flag per staging slot");
 constexpr int64_t kHostChunk = int64_t(1) << 22;  // queries per staged chunk (64 MB of staging)
+// rmq_query_stats' counters: words kStatsSlot .. kStatsSlot + RMQ_QUERY_STATS_FIELDS
+// of the handle's 256-byte counter block (word 0 counts invalid queries)
+constexpr int kStatsSlot = 8;
+static_assert((kStatsSlot + RMQ_QUERY_STATS_FIELDS) * 8 <= 256, "stats fit the counter block");
 }  // namespace
 
 namespace rmq {
@@ -277,6 +281,74 @@ int rmq_probe_gather(const rmq_handle_t *h, const int32_t *d_queries, int64_t q,
     a.invalid = nullptr;
     cudaError_t err = launch_probe_gather(h->plan, a, dev, stream);
     if (err != cudaSuccess) return cuda_fail(err, "rmq_probe_gather: launch");
+    return RMQ_OK;
+}
+
+int rmq_query_stats(const rmq_handle_t *h, const int32_t *d_queries, int64_t q, float *d_val,
+                    int32_t *d_idx, int64_t *h_counts, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_query_stats");
+    g_err[0] = '\0';
+    if (!h || !h_counts) return set_error(RMQ_EINVAL, "rmq_query_stats: NULL argument");
+    if (q < 0) return set_error(RMQ_EINVAL, "rmq_query_stats: q=%lld < 0", (long long)q);
+    for (int c = 0; c < RMQ_QUERY_STATS_FIELDS; ++c) h_counts[c] = 0;
+    if (q == 0) return RMQ_OK;
+    if (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8 != 0)
+        return set_error(RMQ_EINVAL, "rmq_query_stats: d_queries NULL or not 8-byte aligned");
+    if ((d_val && reinterpret_cast<uintptr_t>(d_val) % 4) ||
+        (d_idx && reinterpret_cast<uintptr_t>(d_idx) % 4))
+        return set_error(RMQ_EINVAL, "rmq_query_stats: outputs not 4-byte aligned");
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    if (dev.device != h->device)
+        return set_error(RMQ_EINVAL, "rmq_query_stats: handle built on device %d, current is %d",
+                         h->device, dev.device);
+    // the counters sit in the handle's counter block, after the invalid-query
+    // counter (kStatsSlot words in, RMQ_QUERY_STATS_FIELDS words)
+    unsigned long long *dst = h->invalid + kStatsSlot;
+    QueryArgs a;
+    a.Q = reinterpret_cast<const int2 *>(d_queries);
+    a.q = q;
+    a.val = d_val;
+    a.idx = d_idx;
+    a.invalid = h->invalid;
+    a.stats = dst;
+    unsigned long long host[RMQ_QUERY_STATS_FIELDS];
+    cudaError_t err = cudaMemsetAsync(dst, 0, sizeof(host), stream);
+    if (err == cudaSuccess) err = launch_query(h->plan, a, dev, stream);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(host, dst, sizeof(host), cudaMemcpyDeviceToHost, stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_query_stats");
+    for (int c = 0; c < RMQ_QUERY_STATS_FIELDS; ++c) h_counts[c] = static_cast<int64_t>(host[c]);
+    return RMQ_OK;
+}
+
+int rmq_probe_random(const uint64_t *d_buf, int64_t words, const int32_t *d_queries, int64_t q,
+                     float *d_val, int32_t *d_idx, rmq_stream_t stream) {
+    NvtxRange nvtx_range("rmq_probe_random");
+    g_err[0] = '\0';
+    if (!d_buf || words <= 0 || reinterpret_cast<uintptr_t>(d_buf) % 8 != 0)
+        return set_error(RMQ_EINVAL, "rmq_probe_random: d_buf NULL, unaligned or words <= 0");
+    if (q < 0) return set_error(RMQ_EINVAL, "rmq_probe_random: q=%lld < 0", (long long)q);
+    if (q == 0) return RMQ_OK;
+    if (!d_queries || reinterpret_cast<uintptr_t>(d_queries) % 8 != 0)
+        return set_error(RMQ_EINVAL, "rmq_probe_random: d_queries NULL or not 8-byte aligned");
+    if (!d_val && !d_idx) return set_error(RMQ_EINVAL, "rmq_probe_random: both outputs are NULL");
+    if ((d_val && reinterpret_cast<uintptr_t>(d_val) % 4) ||
+        (d_idx && reinterpret_cast<uintptr_t>(d_idx) % 4))
+        return set_error(RMQ_EINVAL, "rmq_probe_random: outputs not 4-byte aligned");
+    DeviceInfo dev;
+    int rc = device_info(&dev);
+    if (rc) return rc;
+    QueryArgs a;
+    a.Q = reinterpret_cast<const int2 *>(d_queries);
+    a.q = q;
+    a.val = d_val;
+    a.idx = d_idx;
+    a.invalid = nullptr;
+    cudaError_t err = launch_probe_random(reinterpret_cast<const unsigned long long *>(d_buf),
+                                          static_cast<uint64_t>(words), a, dev, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_probe_random: launch");
     return RMQ_OK;
 }
 

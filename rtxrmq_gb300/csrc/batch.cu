@@ -95,6 +95,7 @@ __device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchAr
     v.kmode = kFloatMin;
     v.levels = a.levels;
     v.mlevels = 0u;
+    v.micro_span = 0u;
     return v;
 }
 

@@ -236,16 +236,16 @@ unsigned long long *place_index(BuildPlan &p, void *base_v) {
 }
 
 // The sub-block level works on 32-element micro-blocks aligned in the
-// array, whatever the block size: for a query inside one block with l and r
-// in different micro-blocks, the suffix inside l's micro-block, the prefix
-// inside r's and the whole micro-blocks between all lie in [l, r]. Its
-// table only needs windows as long as a same-block query can span between
-// its two end micro-blocks: bs/32 - 2 when blocks start on micro-block
-// boundaries (bs a multiple of 32), floor((bs + 30) / 32) - 1 otherwise.
+// array, whatever the block size. A query first probes the micro table over
+// every micro-block it touches (a superset of [l, r]; two windows of 2^k
+// micro-blocks cover up to 2^(k+1) - 1 of them), so the table holds windows
+// long enough for any query inside one block: a block touches bs/32
+// micro-blocks when blocks start on micro-block boundaries (bs a multiple
+// of 32), at most floor((bs + 30) / 32) + 1 otherwise.
 uint32_t micro_levels(uint32_t bs) {
     if (bs < 2 * kMicro) return 0;
-    const uint32_t between = (bs % kMicro == 0) ? bs / kMicro - 2 : (bs + kMicro - 2) / kMicro - 1;
-    return between < 1 ? 1u : st_levels(between);
+    const uint32_t touched = (bs % kMicro == 0) ? bs / kMicro : (bs + kMicro - 2) / kMicro + 1;
+    return st_levels(touched);
 }
 
 cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {

@@ -133,6 +133,9 @@ struct QueryArgs {
     float *val;
     int32_t *idx;
     unsigned long long *invalid;  // device counter, may be null
+    // measurement launches only (rmq_query_stats): kStatCount device
+    // counters of how each query was settled; null for every other launch
+    unsigned long long *stats = nullptr;
 };
 cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,
                          cudaStream_t s);
@@ -140,6 +143,9 @@ struct V1View;
 V1View view_of(const BuildPlan &p);
 cudaError_t launch_probe_gather(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,
                                 cudaStream_t s);
+// Random 8-byte loads from buf[0 .. words), query_kernel's grid (rmq_probe_random).
+cudaError_t launch_probe_random(const unsigned long long *buf, uint64_t words, const QueryArgs &a,
+                                const DeviceInfo &dev, cudaStream_t s);
 cudaError_t launch_query_scan(const float *A, uint32_t n, const QueryArgs &a,
                               const DeviceInfo &dev, cudaStream_t s);
 

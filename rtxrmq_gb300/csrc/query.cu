@@ -1,9 +1,9 @@
 // query.cu -- plain query kernels.
 //
 // query_kernel: one CTA answers 256 * QPT consecutive queries at a time with
-// the shared body of query_impl.cuh (RTX_blocks' three-ray decomposition
-// answered from pre/suf/sparse-table lookups, src/rtx_kernels.cu:85-193 and
-// 350-465). Queries and outputs may live in device memory or in pinned host
+// the queued body of query_impl.cuh (RTX_blocks' three-ray decomposition,
+// src/rtx_kernels.cu:85-193 and 350-465, needed only for the queries a
+// probe of the small tables over a superset of [l, r] does not settle). Queries and outputs may live in device memory or in pinned host
 // memory mapped into the device address space: on a Grace-Blackwell node the
 // kernel then streams them over NVLink-C2C while its random lookups hit HBM.
 //
@@ -20,35 +20,67 @@ constexpr int kThreads = 256;
 #define RMQ_QUERY_QPT 2  // queries per thread per step (independent lookups in flight)
 #endif
 constexpr int kQPT = RMQ_QUERY_QPT;
+#ifndef RMQ_QUERY_MINB
+#define RMQ_QUERY_MINB 1  // CTAs per SM the query kernel is compiled for (a register bound)
+#endif
 
-// Grid-stride over steps of 256 * kQPT queries; the next step's queries are
-// loaded before the current step is answered, so their latency (host memory
-// over the host link when called through rmq_query_host) overlaps the
-// current step's lookups.
-template <bool ALIGNED>
-__global__ void __launch_bounds__(kThreads)
-query_kernel(V1View v, QueryOut o, int64_t q) {
-    const int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
+// Queries base + t + k * kThreads (k < kQPT) of a full step, no bounds checks.
+__device__ __forceinline__ void load_full(const QueryOut &o, int64_t base, int2 (&qq)[kQPT]) {
+    const int2 *Qs = o.Q + base;
+#pragma unroll
+    for (int k = 0; k < kQPT; ++k) qq[k] = __ldcs(Qs + threadIdx.x + k * kThreads);
+}
+
+// Grid-stride over steps of 256 * kQPT queries (answer_step_queued); the
+// next step's queries are loaded before the current step is answered, so
+// their latency (host memory over the host link when called through
+// rmq_query_host) overlaps the current step's lookups. Specialised on the
+// key mode and on whether the index has the sub-block level. STATS: the
+// measurement instantiation (rmq_query_stats), which also counts how each
+// query was settled and what it read into stats[kStatCount].
+template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
+__global__ void __launch_bounds__(kThreads, RMQ_QUERY_MINB)
+query_kernel(V1View v, QueryOut o, int64_t q, unsigned long long *stats) {
+    __shared__ MissQueue s_mq[kThreads / 32];
+    constexpr int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * chunk;
     int64_t c0 = static_cast<int64_t>(blockIdx.x) * chunk;
     if (c0 >= q) return;
+    const int64_t last_full = q - chunk;  // steps starting at or before it are full
+    QStats s;
+    if constexpr (STATS)
+        for (int c = 0; c < kStatCount; ++c) s.c[c] = 0u;
+    MissQueue &mq = s_mq[threadIdx.x >> 5];
+    uint32_t waiting = 0;  // the warp's queue length (warp-uniform)
     int2 cur[kQPT];
-    load_queries<kQPT>(o, c0, c0 + chunk < q ? c0 + chunk : q, cur);
+    if (c0 <= last_full)
+        load_full(o, c0, cur);
+    else
+        load_queries<kQPT>(o, c0, q, cur);
     for (; c0 < q; c0 += stride) {
         const int64_t c1 = c0 + stride;
         int2 nxt[kQPT];
-        if (c1 < q) load_queries<kQPT>(o, c1, c1 + chunk < q ? c1 + chunk : q, nxt);
-        answer_step<ALIGNED, kQPT>(v, o, c0, c0 + chunk < q ? c0 + chunk : q, cur);
+        if (c1 <= last_full)
+            load_full(o, c1, nxt);
+        else if (c1 < q)
+            load_queries<kQPT>(o, c1, q, nxt);
+        if (c0 <= last_full)
+            answer_step_queued<ALIGNED, MICRO, MODE, kThreads, kQPT, STATS, true>(
+                v, o, c0, static_cast<uint32_t>(chunk), cur, s, mq, waiting);
+        else
+            answer_step_queued<ALIGNED, MICRO, MODE, kThreads, kQPT, STATS, false>(
+                v, o, c0, static_cast<uint32_t>(q - c0), cur, s, mq, waiting);
 #pragma unroll
         for (int k = 0; k < kQPT; ++k) cur[k] = nxt[k];
     }
+    if (waiting) drain_misses<MODE, STATS>(v, o, mq, waiting, l2_keep_policy(), s);
+    if constexpr (STATS) flush_stats(s, stats);
 }
 
-// Random-access ceiling of query_kernel (rmq_probe_gather): the same grid,
-// query stream and output stores, but per query only the two random
-// 8-byte lookups suf[l] and pre[r] (no block decision, no table probe, no
-// scan). Its rate bounds what any two-lookup query kernel reaches on this
-// index; its answers are not range minima.
+// Random-access ceiling of the un-pruned query on this index
+// (rmq_probe_gather): query_kernel's grid, query stream and output stores,
+// but per query only the two random 8-byte lookups suf[l] and pre[r] (no
+// block decision, no table probe, no scan). Its answers are not range minima.
 __global__ void __launch_bounds__(kThreads)
 gather_kernel(V1View v, QueryOut o, int64_t q) {
     const int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
@@ -68,6 +100,42 @@ gather_kernel(V1View v, QueryOut o, int64_t q) {
         for (int k = 0; k < kQPT; ++k) {
             const int64_t i = c0 + threadIdx.x + static_cast<int64_t>(k) * kThreads;
             if (i < q) put_result(o, i, e[k], v.kmode);
+        }
+    }
+}
+
+// 64-bit finaliser of SplitMix64 (Steele, Lea, Flood, OOPSLA 2014).
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// Random-access rate of this GPU, independent of any index layout
+// (rmq_probe_random): query_kernel's grid, query stream and output stores,
+// and per query two 8-byte loads at positions hashed from (i, l, r),
+// uniform over buf[0 .. words).
+__global__ void __launch_bounds__(kThreads)
+random_gather_kernel(const unsigned long long *__restrict__ buf, uint64_t words, QueryOut o,
+                     int64_t q) {
+    const int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * chunk;
+    for (int64_t c0 = static_cast<int64_t>(blockIdx.x) * chunk; c0 < q; c0 += stride) {
+        int2 qq[kQPT];
+        load_queries<kQPT>(o, c0, c0 + chunk < q ? c0 + chunk : q, qq);
+        Entry e[kQPT];
+#pragma unroll
+        for (int k = 0; k < kQPT; ++k) {
+            const int64_t i = c0 + threadIdx.x + static_cast<int64_t>(k) * kThreads;
+            const uint64_t h1 = mix64((static_cast<uint64_t>(i) << 32) ^ static_cast<uint32_t>(qq[k].x));
+            const uint64_t h2 = mix64(h1 ^ static_cast<uint32_t>(qq[k].y));
+            const uint64_t p1 = __umul64hi(h1, words), p2 = __umul64hi(h2, words);
+            e[k] = better(__ldg(buf + p1), __ldg(buf + p2));
+        }
+#pragma unroll
+        for (int k = 0; k < kQPT; ++k) {
+            const int64_t i = c0 + threadIdx.x + static_cast<int64_t>(k) * kThreads;
+            if (i < q) put_bits_idx(o, i, static_cast<uint32_t>(e[k] >> 32), static_cast<uint32_t>(e[k]));
         }
     }
 }
@@ -95,8 +163,8 @@ scan_kernel(const float *__restrict__ A, uint32_t n, QueryOut o, int64_t q) {
     }
 }
 
-std::atomic<int> g_query_per_sm[2];
 std::atomic<int> g_gather_per_sm{0};
+std::atomic<int> g_random_per_sm{0};
 std::atomic<int> g_scan_per_sm{0};
 
 template <typename K>
@@ -135,7 +203,43 @@ V1View view_of(const BuildPlan &p) {
     v.kmode = p.kmode;
     v.levels = p.levels;
     v.mlevels = p.micro ? p.mlevels : 0u;
+    v.micro_span = p.micro ? (1u << p.mlevels) - 1u : 0u;
     return v;
+}
+
+template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
+cudaError_t launch_query_t(const V1View &v, const QueryOut &o, int64_t q,
+                           unsigned long long *stats, const DeviceInfo &dev, cudaStream_t s) {
+    static std::atomic<int> per_sm_cache{0};
+    int per_sm;
+    const cudaError_t err =
+        occupancy(query_kernel<ALIGNED, MICRO, MODE, STATS>, &per_sm_cache, &per_sm);
+    if (err != cudaSuccess) return err;
+    query_kernel<ALIGNED, MICRO, MODE, STATS>
+        <<<grid_size(q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(v, o, q, stats);
+    return cudaGetLastError();
+}
+
+template <bool ALIGNED, bool MICRO, bool STATS>
+cudaError_t launch_query_m(const V1View &v, const QueryOut &o, int64_t q,
+                           unsigned long long *stats, const DeviceInfo &dev, cudaStream_t s) {
+    switch (v.kmode) {
+    case kFloatMax: return launch_query_t<ALIGNED, MICRO, kFloatMax, STATS>(v, o, q, stats, dev, s);
+    case kIntMin: return launch_query_t<ALIGNED, MICRO, kIntMin, STATS>(v, o, q, stats, dev, s);
+    case kIntMax: return launch_query_t<ALIGNED, MICRO, kIntMax, STATS>(v, o, q, stats, dev, s);
+    default: return launch_query_t<ALIGNED, MICRO, kFloatMin, STATS>(v, o, q, stats, dev, s);
+    }
+}
+
+template <bool STATS>
+cudaError_t launch_query_s(const BuildPlan &p, const V1View &v, const QueryOut &o, int64_t q,
+                           unsigned long long *stats, const DeviceInfo &dev, cudaStream_t s) {
+    const bool micro = v.mst != nullptr;
+    if (p.aligned)
+        return micro ? launch_query_m<true, true, STATS>(v, o, q, stats, dev, s)
+                     : launch_query_m<true, false, STATS>(v, o, q, stats, dev, s);
+    return micro ? launch_query_m<false, true, STATS>(v, o, q, stats, dev, s)
+                 : launch_query_m<false, false, STATS>(v, o, q, stats, dev, s);
 }
 
 cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,
@@ -148,20 +252,24 @@ cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInf
     o.idx = a.idx;
     o.invalid = a.invalid;
     o.span = a.q;
-    cudaError_t err;
-    if (p.aligned) {
-        int per_sm;
-        err = occupancy(query_kernel<true>, &g_query_per_sm[1], &per_sm);
-        if (err != cudaSuccess) return err;
-        query_kernel<true><<<grid_size(a.q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(
-            v, o, a.q);
-    } else {
-        int per_sm;
-        err = occupancy(query_kernel<false>, &g_query_per_sm[0], &per_sm);
-        if (err != cudaSuccess) return err;
-        query_kernel<false><<<grid_size(a.q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(
-            v, o, a.q);
-    }
+    if (a.stats) return launch_query_s<true>(p, v, o, a.q, a.stats, dev, s);
+    return launch_query_s<false>(p, v, o, a.q, nullptr, dev, s);
+}
+
+cudaError_t launch_probe_random(const unsigned long long *buf, uint64_t words, const QueryArgs &a,
+                                const DeviceInfo &dev, cudaStream_t s) {
+    if (a.q <= 0) return cudaSuccess;
+    QueryOut o;
+    o.Q = a.Q;
+    o.val = a.val;
+    o.idx = a.idx;
+    o.invalid = nullptr;
+    o.span = a.q;
+    int per_sm;
+    cudaError_t err = occupancy(random_gather_kernel, &g_random_per_sm, &per_sm);
+    if (err != cudaSuccess) return err;
+    random_gather_kernel<<<grid_size(a.q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(
+        buf, words, o, a.q);
     return cudaGetLastError();
 }
 

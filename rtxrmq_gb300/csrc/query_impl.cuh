@@ -6,17 +6,20 @@
 // query: one through the fully covered blocks lB+1..rB-1, one through the
 // left partial block and one through the right partial block, and keeps the
 // closest hit. Here the same decomposition is answered from arrays:
-//   left partial block   -> suf[l]
-//   right partial block  -> pre[r]
+//   left partial block   -> suf[l]   (random HBM lookup)
+//   right partial block  -> pre[r]   (random HBM lookup)
 //   full blocks between  -> two sparse-table entries (L2-resident)
-// A query inside one block (the reference's single-ray case,
-// src/rtx_kernels.cu:116-135) is answered from pre/suf when it touches a
-// block edge; otherwise through the sub-block level when the index has one
-// (32-element micro-blocks: msuf[l], mpre[r] and two micro-table entries, or
-// one thread's scan of a single 128-byte line), and by a warp-cooperative
-// scan of A[l..r] reducing the composites with __reduce_min_sync when it
-// does not. All comparisons are unsigned minima of the composites of
-// common.cuh; only the final answer is decoded.
+// and it is needed only for the few queries a cheaper test does not settle:
+// every query first probes a small L2-resident table over all the units it
+// touches (blocks lB..rB, or with the sub-block level the 32-element
+// micro-blocks l/32..r/32), and when the leftmost best of that superset
+// lies inside [l, r] it is the answer without any per-element lookup. A
+// query inside one micro-block is settled by one thread's scan of that
+// 128-byte line; without the sub-block level a query inside one block that
+// the probe does not settle reads pre / suf at a block edge, or is scanned
+// by the whole warp (__reduce_min_sync over the composites). All
+// comparisons are unsigned minima of the composites of common.cuh; only the
+// final answer is decoded.
 //
 // Differences from the reference kept on purpose: ties between rays are
 // resolved leftmost (the reference compares rays with strict `<` in the
@@ -55,6 +58,9 @@ struct V1View {
     uint32_t kmode;     // KeyMode: element type and minimum / maximum
     uint32_t levels;    // sparse-table levels (st holds levels * nb entries)
     uint32_t mlevels;   // micro-table levels (moff holds mlevels - 1 rows of nmicro)
+    // 2^mlevels - 1: a query whose end micro-blocks ml < mr have
+    // mr - ml < micro_span is probed through the micro table (0: no micro level)
+    uint32_t micro_span;
 };
 
 // Range-checked accesses (rmq_chk, common.cuh): element loads by absolute
@@ -77,13 +83,11 @@ __device__ __forceinline__ Entry ld_entry_cs(const Entry *t, uint64_t i, uint64_
                              : kEntryNone;
 }
 
-// The tables a query reads beside its two random per-element lookups (the
-// sparse table over block minima, the micro table) are small; their loads
-// carry an L2 evict-last policy (PTX createpolicy + ld.L2::cache_hint) so
-// that the per-element lines streaming through L2 evict them last. No L2
-// carve-out is set aside, unlike a persisting access-policy window. The
-// policy is made at each load: holding it across the step costs registers
-// (and resident CTAs) for nothing measurable.
+// The small tables every query probes (the sparse table over block minima,
+// the micro table) are read with an L2 evict-last policy (PTX createpolicy +
+// ld.L2::cache_hint), so that the per-element lines and the query stream
+// passing through L2 evict them last. No L2 carve-out is set aside, unlike a
+// persisting access-policy window. The policy is made once per step.
 __device__ __forceinline__ uint64_t l2_keep_policy() {
     uint64_t p;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
@@ -114,41 +118,39 @@ __device__ __forceinline__ uint32_t ld_moff(const V1View &v, uint64_t i, uint64_
     return r;
 }
 
-// Leftmost minimum of local A[a..b] (b - a < 32, at most 9 16-byte loads)
-// computed by one thread.
+// Leftmost minimum of local A[a..b] (b - a < 32) computed by one thread.
+// ALIGNED: 16-byte loads of the chunks covering [a, b] (at most 9), two per
+// round, so that few registers are live.
 template <bool ALIGNED>
-__device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, uint32_t b) {
+__device__ __forceinline__ Entry thread_range_min(const V1View &v, uint32_t a, uint32_t b,
+                                                  uint32_t mode) {
     const int64_t aa = v.off + a, ab = v.off + b;
     Entry best = kEntryNone;
     if (ALIGNED) {
-        const int64_t p0 = aa & ~int64_t(3);
+#pragma unroll 2
+        for (int64_t p = aa & ~int64_t(3); p <= ab; p += 4) {
+            uint32_t w[4];
+            if (p + 3 < v.limit) {
+                const uint4 f = ld_elem4(v, p);
+                w[0] = f.x;
+                w[1] = f.y;
+                w[2] = f.z;
+                w[3] = f.w;
+            } else {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const int64_t p = p0 + 4 * k;
-            if (p <= ab) {
-                uint32_t w[4];
-                if (p + 3 < v.limit) {
-                    const uint4 f = ld_elem4(v, p);
-                    w[0] = f.x;
-                    w[1] = f.y;
-                    w[2] = f.z;
-                    w[3] = f.w;
-                } else {
+                for (int c = 0; c < 4; ++c)
+                    w[c] = (p + c <= ab) ? ld_elem(v, p + c) : 0u;
+            }
 #pragma unroll
-                    for (int c = 0; c < 4; ++c)
-                        w[c] = (p + c <= ab) ? ld_elem(v, p + c) : 0u;
-                }
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const int64_t g = p + c;
-                    if (g >= aa && g <= ab)
-                        best = better(best, make_entry(w[c], static_cast<uint32_t>(g - v.off), v.kmode));
-                }
+            for (int c = 0; c < 4; ++c) {
+                const int64_t g = p + c;
+                if (g >= aa && g <= ab)
+                    best = better(best, make_entry(w[c], static_cast<uint32_t>(g - v.off), mode));
             }
         }
     } else {
         for (int64_t g = aa; g <= ab; ++g)
-            best = better(best, make_entry(ld_elem(v, g), static_cast<uint32_t>(g - v.off), v.kmode));
+            best = better(best, make_entry(ld_elem(v, g), static_cast<uint32_t>(g - v.off), mode));
     }
     return best;
 }
@@ -184,7 +186,7 @@ __device__ __forceinline__ void put_invalid(const QueryOut &o, int64_t i) {
 // buffer base is 16-byte aligned, so 16-byte loads on absolute indices are.
 template <bool ALIGNED>
 __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, uint32_t r,
-                                                 int lane) {
+                                                 int lane, uint32_t mode) {
     Entry best = kEntryNone;
     const int64_t al = v.off + l, ar = v.off + r;
     if (ALIGNED) {
@@ -205,12 +207,12 @@ __device__ __forceinline__ Entry warp_scan_range(const V1View &v, uint32_t l, ui
             for (int c = 0; c < 4; ++c) {
                 const int64_t g = p + c;
                 if (g >= al && g <= ar)
-                    best = better(best, make_entry(b[c], static_cast<uint32_t>(g - v.off), v.kmode));
+                    best = better(best, make_entry(b[c], static_cast<uint32_t>(g - v.off), mode));
             }
         }
     } else {
         for (int64_t g = al + lane; g <= ar; g += 32)
-            best = better(best, make_entry(ld_elem(v, g), static_cast<uint32_t>(g - v.off), v.kmode));
+            best = better(best, make_entry(ld_elem(v, g), static_cast<uint32_t>(g - v.off), mode));
     }
     // 64-bit minimum across the warp: the key word first, then the low word
     // among the lanes that hold that key
@@ -240,119 +242,510 @@ __device__ __forceinline__ void load_queries(const QueryOut &o, int64_t base, in
     }
 }
 
-// One step of the CTA: the QPT * blockDim.x queries starting at `base`,
-// already loaded into qq. Uniform across the CTA (warp-cooperative scans
-// need full warps).
-template <bool ALIGNED, int QPT>
+// ---- per-query work --------------------------------------------------------
+//
+// Every probe of a small table returns the leftmost best element of a set of
+// whole units (blocks of the sparse table, micro-blocks of the micro table)
+// that contains [l, r]. If that element's index lies in [l, r], it is the
+// answer: it beats every element of the superset, and an equal element
+// further left inside [l, r] would have been chosen instead. Otherwise the
+// best lies outside on one side, say left of l in unit a; then the answer is
+// better(S[l], best of units a+1..b) when the latter falls at or before r
+// (S[l] covers [l, end of a]), and the three-part decomposition of the
+// reference (left partial, units between, right partial) only when it does
+// not. The per-element entries S / P, the random HBM lookups, are read only
+// on those two fallbacks.
+
+// Query counters of a measurement launch (rmq_query_stats); the normal
+// kernels compile them out.
+enum QStat : int {
+    kStatFirst = 0,   // settled by the superset probe
+    kStatSecond,      // settled by the second probe and one per-element entry
+    kStatFull,        // three-part decomposition: two entries and a middle probe
+    kStatMicroScan,   // inside one micro-block: one thread scans its line
+    kStatBlockEdge,   // one block, no sub-block level: pre / suf at a block edge
+    kStatWarpScan,    // one block, no sub-block level: warp-cooperative scan
+    kStatEntries,     // per-element entries read (pre, suf, mpre, msuf)
+    kStatTable,       // small-table words read (sparse table, micro offsets and minima)
+    kStatSectors,     // 32-byte sectors of A read by scans
+    kStatInvalid,     // invalid queries
+    kStatCount
+};
+struct QStats {
+    uint32_t c[kStatCount];
+};
+
+// Leftmost best of blocks a..b (a <= b < nb) from the sparse table: two
+// entries of level floor(log2(b - a + 1)), one when the window is exact.
+template <bool STATS>
+__device__ __forceinline__ Entry st_probe(const V1View &v, uint32_t a, uint32_t b, uint64_t pol,
+                                          QStats &s) {
+    const int lev = ilog2(b - a + 1u);
+    const uint64_t row = static_cast<uint64_t>(lev) * v.nb;
+    const uint64_t size = static_cast<uint64_t>(v.levels) * v.nb;
+    const uint32_t c = b + 1u - (1u << lev);
+    const Entry x = ld_entry_keep(v.st, row + a, size, pol);
+    Entry y = x;
+    if (c != a) y = ld_entry_keep(v.st, row + c, size, pol);
+    if constexpr (STATS) s.c[kStatTable] += (c != a) ? 2u : 1u;
+    return better(x, y);
+}
+
+// Leftmost best of micro-blocks a..b (a <= b, b - a + 1 < 2^mlevels): the
+// offsets of the two windows' best micro-blocks, then their minima.
+template <bool STATS>
+__device__ __forceinline__ Entry micro_probe(const V1View &v, uint32_t a, uint32_t b, uint64_t pol,
+                                             QStats &s) {
+    const int lev = ilog2(b - a + 1u);
+    uint32_t x = a, y = b + 1u - (1u << lev);
+    if (lev > 0) {
+        const uint64_t row = static_cast<uint64_t>(lev - 1) * v.nmicro;
+        const bool two = y != x;
+        const uint32_t ox = ld_moff(v, row + x, pol);
+        const uint32_t oy = two ? ld_moff(v, row + y, pol) : ox;
+        if constexpr (STATS) s.c[kStatTable] += two ? 2u : 1u;
+        x += ox;
+        y += oy;
+    }
+    const Entry ex = ld_entry_keep(v.mst, x, v.nmicro, pol);
+    Entry ey = ex;
+    if (y != x) ey = ld_entry_keep(v.mst, y, v.nmicro, pol);
+    if constexpr (STATS) s.c[kStatTable] += (y != x) ? 2u : 1u;
+    return better(ex, ey);
+}
+
+template <bool STATS>
+__device__ __forceinline__ Entry unit_probe(const V1View &v, bool micro, uint32_t a, uint32_t b,
+                                            uint64_t pol, QStats &s) {
+    return micro ? micro_probe<STATS>(v, a, b, pol, s) : st_probe<STATS>(v, a, b, pol, s);
+}
+
+// S[l]: best of A[l .. end of l's unit]; P[r]: best of A[start of r's unit .. r].
+// The micro-level entries are read with streaming loads (they are read once,
+// and would otherwise push the micro table out of L2).
+template <bool STATS>
+__device__ __forceinline__ Entry left_entry(const V1View &v, bool micro, uint32_t l, QStats &s) {
+    if constexpr (STATS) s.c[kStatEntries] += 1u;
+    return micro ? ld_entry_cs(v.msuf, l, v.n) : ld_entry(v.suf, l, v.n);
+}
+template <bool STATS>
+__device__ __forceinline__ Entry right_entry(const V1View &v, bool micro, uint32_t r, QStats &s) {
+    if constexpr (STATS) s.c[kStatEntries] += 1u;
+    return micro ? ld_entry_cs(v.mpre, r, v.n) : ld_entry(v.pre, r, v.n);
+}
+
+// 32-byte sectors of the local range A[a..b]
+__device__ __forceinline__ uint32_t range_sectors(const V1View &v, uint32_t a, uint32_t b) {
+    return static_cast<uint32_t>(((v.off + b) >> 3) - ((v.off + a) >> 3) + 1);
+}
+
+enum : uint32_t {
+    kPathNone = 0,    // not a query of this step, or invalid
+    kPathTable,       // superset probe over blocks lB..rB
+    kPathMicroTable,  // superset probe over micro-blocks ml..mr
+    kPathMicroScan,   // inside one micro-block
+    kPathBlock,       // one block, no sub-block level
+    kPathWarpScan,    // left for the warp-cooperative scan
+};
+
+// One step of the CTA (the batch kernel's query phase): the QPT *
+// blockDim.x queries starting at `base`, already loaded into qq. Three
+// rounds of loads, each issued for all QPT queries of the thread before any
+// result is used: the superset probes; for the queries they do not settle,
+// the one per-element entry that is needed in any case and a narrower
+// probe; for the few still open, the rest of the three-part decomposition.
+// Uniform across the CTA (warp-cooperative scans need full warps).
+template <bool ALIGNED, int QPT, bool STATS>
 __device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, int64_t base,
-                                            int64_t q1, const int2 (&qq)[QPT]) {
+                                            int64_t q1, const int2 (&qq)[QPT], QStats &s) {
     const int lane = threadIdx.x & 31;
-    {
-        uint32_t l[QPT], r[QPT];
-        bool act[QPT], ok[QPT], scan[QPT];
-        Entry es[QPT], ep[QPT], ea[QPT], eb[QPT];
+    const uint64_t pol = l2_keep_policy();
+    uint32_t l[QPT], r[QPT], a[QPT], b[QPT], path[QPT], side[QPT];
+    bool act[QPT];
+    Entry res[QPT], e1[QPT], e2[QPT];
+
+    // round 1: classify, probe the superset
 #pragma unroll
-        for (int k = 0; k < QPT; ++k) {
-            const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
-            act[k] = i < q1;
-            ok[k] = act[k] && qq[k].x >= 0 && qq[k].x <= qq[k].y &&
-                    static_cast<uint32_t>(qq[k].y) < v.n;
-            l[k] = ok[k] ? static_cast<uint32_t>(qq[k].x) : 0u;
-            r[k] = ok[k] ? static_cast<uint32_t>(qq[k].y) : 0u;
+    for (int k = 0; k < QPT; ++k) {
+        const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
+        act[k] = i < q1;
+        const bool ok = act[k] && qq[k].x >= 0 && qq[k].x <= qq[k].y &&
+                        static_cast<uint32_t>(qq[k].y) < v.n;
+        l[k] = ok ? static_cast<uint32_t>(qq[k].x) : 0u;
+        r[k] = ok ? static_cast<uint32_t>(qq[k].y) : 0u;
+        const uint32_t lB = div31(l[k], v.dv), rB = div31(r[k], v.dv);
+        const uint32_t ml = l[k] >> 5, mr = r[k] >> 5;
+        path[k] = kPathNone;
+        a[k] = lB;
+        b[k] = rB;
+        side[k] = 0u;
+        res[k] = kEntryNone;
+        e1[k] = kEntryNone;
+        e2[k] = kEntryNone;
+        if (ok) {
+            if (v.mst && ml == mr) {
+                path[k] = kPathMicroScan;
+            } else if (v.mst && ilog2(mr - ml + 1u) < static_cast<int>(v.mlevels)) {
+                path[k] = kPathMicroTable;
+                a[k] = ml;
+                b[k] = mr;
+            } else {
+                path[k] = lB != rB ? kPathTable : kPathBlock;
+            }
+        } else if (act[k]) {
+            if constexpr (STATS) s.c[kStatInvalid] += 1u;
         }
+        if (path[k] == kPathTable || path[k] == kPathBlock || path[k] == kPathMicroTable)
+            res[k] = unit_probe<STATS>(v, path[k] == kPathMicroTable, a[k], b[k], pol, s);
+    }
+
+    // round 2: queries whose superset best lies outside [l, r]
 #pragma unroll
-        for (int k = 0; k < QPT; ++k) {
-            const uint32_t lB = div31(l[k], v.dv);
-            const uint32_t rB = div31(r[k], v.dv);
-            const bool cross = ok[k] && lB != rB;
-            const uint32_t bstart = lB * v.bs;
+    for (int k = 0; k < QPT; ++k) {
+        if (path[k] != kPathTable && path[k] != kPathBlock && path[k] != kPathMicroTable) continue;
+        const uint32_t m = entry_idx(res[k]);
+        if (m >= l[k] && m <= r[k]) {
+            if constexpr (STATS) s.c[kStatFirst] += 1u;
+            continue;
+        }
+        if (path[k] == kPathBlock) {
+            // one block without the sub-block level: its suffix entry at l is
+            // exact when r ends the block, its prefix entry at r when l starts it
+            const uint32_t bstart = a[k] * v.bs;
             const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
-            const bool same = ok[k] && lB == rB;
-            const bool use_suf = cross || (same && r[k] == bend);
-            const bool use_pre = cross || (same && l[k] == bstart);
-            scan[k] = same && !use_suf && !use_pre;
-            es[k] = use_suf ? ld_entry(v.suf, l[k], v.n) : kEntryNone;
-            ep[k] = use_pre ? ld_entry(v.pre, r[k], v.n) : kEntryNone;
-            ea[k] = kEntryNone;
-            eb[k] = kEntryNone;
-            if (cross && rB - lB >= 2u) {
-                const uint32_t lo = lB + 1u, hi = rB - 1u;
-                const int lev = ilog2(hi - lo + 1u);
-                const uint64_t row = static_cast<uint64_t>(lev) * v.nb;
-                const uint64_t size = static_cast<uint64_t>(v.levels) * v.nb;
-                ea[k] = ld_entry_keep(v.st, row + lo, size, l2_keep_policy());
-                eb[k] = ld_entry_keep(v.st, row + hi + 1u - (1u << lev), size, l2_keep_policy());
+            if (r[k] == bend) {
+                res[k] = left_entry<STATS>(v, false, l[k], s);
+            } else if (l[k] == bstart) {
+                res[k] = right_entry<STATS>(v, false, r[k], s);
+            } else {
+                path[k] = kPathWarpScan;
+                continue;
             }
-            if (v.mst && scan[k] && (l[k] >> 5) != (r[k] >> 5)) {
-                // same block through the sub-block level, issued here beside the
-                // other queries' lookups so that all of them are in flight at
-                // once: the partial micro-blocks at both ends from the
-                // in-micro-block suffix / prefix minima, the micro-blocks between
-                // from the micro table (two offsets, then the two minima they
-                // point at; L2-resident). Only a query inside one micro-block
-                // is left to scan.
-                const uint32_t ml = l[k] >> 5, mr = r[k] >> 5;
-                es[k] = ld_entry_cs(v.msuf, l[k], v.n);
-                ep[k] = ld_entry_cs(v.mpre, r[k], v.n);
-                if (mr - ml >= 2u) {
-                    const uint32_t lo = ml + 1u, hi = mr - 1u;
-                    const int lev = ilog2(hi - lo + 1u);
-                    uint32_t a = lo, b = hi + 1u - (1u << lev);
-                    if (lev > 0) {
-                        const uint64_t row = static_cast<uint64_t>(lev - 1) * v.nmicro;
-                        a += ld_moff(v, row + a, l2_keep_policy());
-                        b += ld_moff(v, row + b, l2_keep_policy());
-                    }
-                    ea[k] = ld_entry_keep(v.mst, a, v.nmicro, l2_keep_policy());
-                    eb[k] = ld_entry_keep(v.mst, b, v.nmicro, l2_keep_policy());
-                }
-                scan[k] = false;
-            }
+            if constexpr (STATS) s.c[kStatBlockEdge] += 1u;
+            continue;
         }
-        if (v.mst) {
-            // sub-block level: every query of the step is answered by its own
-            // thread (a query inside one micro-block scans that micro-block's
-            // line), so each result is stored once and a warp's 128-byte
-            // output line is written by one instruction (partial-line writes
-            // cost extra transactions, most of all to host memory)
+        const bool micro = path[k] == kPathMicroTable;
+        if (m < l[k]) {
+            side[k] = 1u;
+            e1[k] = left_entry<STATS>(v, micro, l[k], s);
+            e2[k] = unit_probe<STATS>(v, micro, a[k] + 1u, b[k], pol, s);
+        } else {
+            side[k] = 2u;
+            e1[k] = right_entry<STATS>(v, micro, r[k], s);
+            e2[k] = unit_probe<STATS>(v, micro, a[k], b[k] - 1u, pol, s);
+        }
+    }
+
+    // round 3: the narrower probe decides whether the other per-element
+    // entry and the middle units are needed
 #pragma unroll
-            for (int k = 0; k < QPT; ++k) {
-                if (!act[k]) continue;
-                const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
-                if (!ok[k]) {
-                    put_invalid(o, i);
-                    continue;
-                }
-                const Entry e = scan[k] ? thread_range_min<ALIGNED>(v, l[k], r[k])
-                                        : better(better(es[k], ep[k]), better(ea[k], eb[k]));
-                put_result(o, i, e, v.kmode);
-            }
-            return;
+    for (int k = 0; k < QPT; ++k) {
+        if (!side[k]) continue;
+        const bool micro = path[k] == kPathMicroTable;
+        const uint32_t m2 = entry_idx(e2[k]);
+        if (side[k] == 1u ? m2 <= r[k] : m2 >= l[k]) {
+            res[k] = better(e1[k], e2[k]);
+            if constexpr (STATS) s.c[kStatSecond] += 1u;
+        } else {
+            const Entry mid = (b[k] - a[k] >= 2u)
+                                  ? unit_probe<STATS>(v, micro, a[k] + 1u, b[k] - 1u, pol, s)
+                                  : kEntryNone;
+            const Entry other = side[k] == 1u ? right_entry<STATS>(v, micro, r[k], s)
+                                              : left_entry<STATS>(v, micro, l[k], s);
+            res[k] = better(better(e1[k], other), mid);
+            if constexpr (STATS) s.c[kStatFull] += 1u;
         }
+    }
+
+    // results: every query but the warp-scanned ones by its own thread, so a
+    // warp's 128-byte output line is written by one instruction (partial-line
+    // writes cost extra transactions, most of all to host memory)
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+        if (!act[k] || path[k] == kPathWarpScan) continue;
+        const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
+        if (path[k] == kPathNone) {
+            put_invalid(o, i);
+            continue;
+        }
+        if (path[k] == kPathMicroScan) {
+            res[k] = thread_range_min<ALIGNED>(v, l[k], r[k], v.kmode);
+            if constexpr (STATS) {
+                s.c[kStatMicroScan] += 1u;
+                s.c[kStatSectors] += range_sectors(v, l[k], r[k]);
+            }
+        }
+        put_result(o, i, res[k], v.kmode);
+    }
+
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+        unsigned mask = __ballot_sync(0xffffffffu, path[k] == kPathWarpScan);
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1u;
+            const uint32_t ls = __shfl_sync(0xffffffffu, l[k], src);
+            const uint32_t rs = __shfl_sync(0xffffffffu, r[k], src);
+            const Entry e = warp_scan_range<ALIGNED>(v, ls, rs, lane, v.kmode);
+            if (lane == src) {
+                put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e,
+                           v.kmode);
+                if constexpr (STATS) {
+                    s.c[kStatWarpScan] += 1u;
+                    s.c[kStatSectors] += range_sectors(v, ls, rs);
+                }
+            }
+        }
+    }
+}
+
+// ---- the queued form (query_kernel) -----------------------------------------
+//
+// answer_step settles a query that its probe leaves open inside the same
+// step, so a warp waits for the slowest lane's chain of dependent loads
+// (entry, narrower probe, then maybe the rest), and it carries every path's
+// state for every query. The queued form is specialised at compile time
+// on the key mode and on whether the index has the sub-block level, and
+// its main pass does only the superset probe: a query the probe settles is
+// stored at once; one it leaves open goes into a per-warp queue in shared
+// memory, and whenever 32 are waiting the warp settles them together, one
+// per lane (finish_miss).
+
+// code of a queued query: its path, and kMissLeft when the probe's best
+// lay left of l (else right of r)
+constexpr uint32_t kMissLeft = 8u;
+
+// Rounds 2 and 3 of answer_step for one query whose superset best lay
+// outside [l, r] (or, without the sub-block level, inside one block at an
+// edge): the per-element entry on that side and a narrower probe, then
+// only if needed the other entry and the middle units.
+template <bool STATS>
+__device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32_t r,
+                                             uint32_t code, uint64_t pol, QStats &s) {
+    const uint32_t path = code & 7u;
+    if (path == kPathBlock) {
+        if constexpr (STATS) s.c[kStatBlockEdge] += 1u;
+        const uint32_t bstart = div31(l, v.dv) * v.bs;
+        const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
+        return r == bend ? left_entry<STATS>(v, false, l, s) : right_entry<STATS>(v, false, r, s);
+    }
+    const bool micro = path == kPathMicroTable;
+    const uint32_t a = micro ? (l >> 5) : div31(l, v.dv);
+    const uint32_t b = micro ? (r >> 5) : div31(r, v.dv);
+    const bool left = (code & kMissLeft) != 0u;
+    const Entry e1 = left ? left_entry<STATS>(v, micro, l, s) : right_entry<STATS>(v, micro, r, s);
+    const Entry e2 = left ? unit_probe<STATS>(v, micro, a + 1u, b, pol, s)
+                          : unit_probe<STATS>(v, micro, a, b - 1u, pol, s);
+    const uint32_t m2 = entry_idx(e2);
+    if (left ? m2 <= r : m2 >= l) {
+        if constexpr (STATS) s.c[kStatSecond] += 1u;
+        return better(e1, e2);
+    }
+    if constexpr (STATS) s.c[kStatFull] += 1u;
+    const Entry mid = (b - a >= 2u) ? unit_probe<STATS>(v, micro, a + 1u, b - 1u, pol, s)
+                                    : kEntryNone;
+    const Entry other = left ? right_entry<STATS>(v, micro, r, s) : left_entry<STATS>(v, micro, l, s);
+    return better(better(e1, other), mid);
+}
+
+// One warp's queue: up to 31 waiting queries plus the 32 that one query
+// slot of a step can add.
+struct MissQueue {
+    static constexpr int kCap = 64;
+    int64_t qi[kCap];
+    uint32_t l[kCap];
+    uint32_t r[kCap];
+    uint8_t code[kCap];
+};
+
+// Settles the last min(count, 32) queued queries, one per lane; the whole
+// warp calls it (count is warp-uniform).
+template <uint32_t MODE, bool STATS>
+__device__ __forceinline__ void drain_misses(const V1View &v, const QueryOut &o, MissQueue &mq,
+                                             uint32_t &count, uint64_t pol, QStats &s) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t take = count < 32u ? count : 32u;
+    __syncwarp();
+    if (lane < take) {
+        const uint32_t e = count - take + lane;
+        const Entry r = finish_miss<STATS>(v, mq.l[e], mq.r[e], mq.code[e], pol, s);
+        put_result(o, mq.qi[e], r, MODE);
+    }
+    __syncwarp();
+    count -= take;
+}
+
+// The bits of an entry's element for key mode MODE, without branches
+// (unkey for a mode known at compile time).
+template <uint32_t MODE>
+__device__ __forceinline__ uint32_t decode_bits(Entry e) {
+    const uint32_t k = static_cast<uint32_t>(e >> 32);
+    if constexpr (MODE == kIntMin) {
+        return k ^ 0x80000000u;
+    } else if constexpr (MODE == kIntMax) {
+        return k ^ 0x7fffffffu;
+    } else {
+        const uint32_t nz = static_cast<uint32_t>(e) & 1u;
+        // f = fkey(bits): bits | 2^31 for a positive value (2^31 for +-0,
+        // negzero telling them apart), ~bits for a negative one
+        const uint32_t f = (MODE == kFloatMax) ? ~k : k;
+        const uint32_t b = (f & 0x80000000u) ? ((f & 0x7fffffffu) | (nz << 31)) : ~f;
+        return k == 0xffffffffu ? 0x7fc00000u : b;  // NaN: the canonical quiet NaN
+    }
+}
+
+// The superset probe of the queued form for a valid query not inside one
+// micro-block: through the micro table when the query's micro-blocks fit
+// it (`mic`), else through the block table. One straight sequence: the
+// unit, level and table are selected, and only the micro table's offset
+// loads sit behind a branch.
+template <bool MICRO, bool STATS>
+__device__ __forceinline__ Entry superset_probe(const V1View &v, uint32_t l, uint32_t r,
+                                                uint64_t pol, QStats &s, bool &mic) {
+    const uint32_t ml = l >> 5, mr = r >> 5;
+    mic = MICRO && mr - ml < v.micro_span;
+    const uint32_t a = mic ? ml : div31(l, v.dv);
+    const uint32_t b = mic ? mr : div31(r, v.dv);
+    const int lev = ilog2(b - a + 1u);
+    uint32_t x = a, y = b + 1u - (1u << lev);
+    if (MICRO && mic) {
+        // lev >= 1: the query spans at least two micro-blocks
+        const uint64_t row = static_cast<uint64_t>(lev - 1) * v.nmicro;
+        x += ld_moff(v, row + x, pol);
+        y += ld_moff(v, row + y, pol);
+        if constexpr (STATS) s.c[kStatTable] += 2u;
+    }
+    const Entry *t = mic ? v.mst : v.st + static_cast<uint64_t>(lev) * v.nb;
+    const uint64_t size = mic ? v.nmicro : static_cast<uint64_t>(v.levels - lev) * v.nb;
+    const Entry e1 = ld_entry_keep(t, x, size, pol);
+    const Entry e2 = ld_entry_keep(t, y, size, pol);
+    if constexpr (STATS) s.c[kStatTable] += 2u;
+    return better(e1, e2);
+}
+
+// One step of the queued form over queries [base, base + cnt) (cnt <=
+// THREADS * QPT): thread t handles base + t + k * THREADS, already loaded
+// into qq. FULL: cnt == THREADS * QPT, so no query needs a bounds check.
+// MICRO: the index has the sub-block level (then every query inside one
+// block spans few enough micro-blocks for the micro table, and only the
+// block table serves longer ones). `count` carries the warp's queue length
+// from step to step; the caller drains the rest.
+template <bool ALIGNED, bool MICRO, uint32_t MODE, int THREADS, int QPT, bool STATS, bool FULL>
+__device__ __forceinline__ void answer_step_queued(const V1View &v, const QueryOut &o,
+                                                   int64_t base, uint32_t cnt,
+                                                   const int2 (&qq)[QPT], QStats &s,
+                                                   MissQueue &mq, uint32_t &count) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t pol = l2_keep_policy();
+    float *const vs = o.val ? o.val + base : nullptr;
+    int32_t *const is = o.idx ? o.idx + base : nullptr;
+    Entry res[QPT];
+    bool ok[QPT], scan[QPT], mic[QPT];
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+        const uint32_t j = threadIdx.x + k * THREADS;
+        const uint32_t l = static_cast<uint32_t>(qq[k].x), r = static_cast<uint32_t>(qq[k].y);
+        ok[k] = (FULL || j < cnt) && qq[k].x >= 0 && l <= r && r < v.n;
+        scan[k] = MICRO && (l >> 5) == (r >> 5);
+        mic[k] = false;
+        res[k] = kEntryNone;
+        if (ok[k] && !scan[k]) res[k] = superset_probe<MICRO, STATS>(v, l, r, pol, s, mic[k]);
+    }
+    bool miss[QPT];
+    bool any_miss = false;
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+        const uint32_t j = threadIdx.x + k * THREADS;
+        const uint32_t l = static_cast<uint32_t>(qq[k].x), r = static_cast<uint32_t>(qq[k].y);
+        miss[k] = false;
+        if (!ok[k]) {
+            if (FULL || j < cnt) {
+                put_invalid(o, base + j);
+                if constexpr (STATS) s.c[kStatInvalid] += 1u;
+            }
+            continue;
+        }
+        if (MICRO && scan[k]) {
+            res[k] = thread_range_min<ALIGNED>(v, l, r, MODE);
+            if constexpr (STATS) {
+                s.c[kStatMicroScan] += 1u;
+                s.c[kStatSectors] += range_sectors(v, l, r);
+            }
+        } else {
+            miss[k] = entry_idx(res[k]) - l > r - l;
+            if constexpr (STATS) s.c[kStatFirst] += miss[k] ? 0u : 1u;
+        }
+        any_miss |= miss[k];
+        // the probe's answer is stored even for a query it leaves open: the
+        // drain (same warp, after __syncwarp) or the warp scan (same thread)
+        // overwrites it, and whole-warp stores keep the output lines whole
+        if (vs) __stcs(reinterpret_cast<unsigned int *>(vs) + j, decode_bits<MODE>(res[k]));
+        if (is) __stcs(is + j, static_cast<int32_t>(entry_idx(res[k])));
+    }
+    if (!__any_sync(0xffffffffu, any_miss)) return;
+    bool wscan[QPT];
+#pragma unroll
+    for (int k = 0; k < QPT; ++k) {
+        const uint32_t l = static_cast<uint32_t>(qq[k].x), r = static_cast<uint32_t>(qq[k].y);
+        uint32_t code = mic[k] ? kPathMicroTable : kPathTable;
+        wscan[k] = false;
+        if (!MICRO && miss[k]) {
+            const uint32_t lB = div31(l, v.dv);
+            if (lB == div31(r, v.dv)) {
+                // one block without the sub-block level: an edge entry when the
+                // query touches the block's edge, else the warp scans it
+                const uint32_t bstart = lB * v.bs;
+                const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
+                code = kPathBlock;
+                if (r != bend && l != bstart) {
+                    miss[k] = false;
+                    wscan[k] = true;
+                }
+            }
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, miss[k]);
+        if (miss[k]) {
+            const uint32_t e = count + __popc(mask & ((1u << lane) - 1u));
+            if (code != kPathBlock && entry_idx(res[k]) < l) code |= kMissLeft;
+            mq.qi[e] = base + threadIdx.x + k * THREADS;
+            mq.l[e] = l;
+            mq.r[e] = r;
+            mq.code[e] = static_cast<uint8_t>(code);
+        }
+        count += __popc(mask);
+        if (count >= 32u) drain_misses<MODE, STATS>(v, o, mq, count, pol, s);
+    }
+    if constexpr (!MICRO) {
 #pragma unroll
         for (int k = 0; k < QPT; ++k) {
-            if (act[k] && !scan[k]) {
-                const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
-                if (ok[k])
-                    put_result(o, i, better(better(es[k], ep[k]), better(ea[k], eb[k])), v.kmode);
-                else
-                    put_invalid(o, i);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < QPT; ++k) {
-            unsigned mask = __ballot_sync(0xffffffffu, scan[k]);
+            unsigned mask = __ballot_sync(0xffffffffu, wscan[k]);
             while (mask) {
                 const int src = __ffs(mask) - 1;
                 mask &= mask - 1u;
-                const uint32_t ls = __shfl_sync(0xffffffffu, l[k], src);
-                const uint32_t rs = __shfl_sync(0xffffffffu, r[k], src);
-                const Entry e = warp_scan_range<ALIGNED>(v, ls, rs, lane);
-                if (lane == src)
-                    put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e,
-                               v.kmode);
+                const uint32_t ls = __shfl_sync(0xffffffffu, static_cast<uint32_t>(qq[k].x), src);
+                const uint32_t rs = __shfl_sync(0xffffffffu, static_cast<uint32_t>(qq[k].y), src);
+                const Entry e = warp_scan_range<ALIGNED>(v, ls, rs, static_cast<int>(lane), MODE);
+                if (static_cast<int>(lane) == src) {
+                    put_result(o, base + threadIdx.x + k * THREADS, e, MODE);
+                    if constexpr (STATS) {
+                        s.c[kStatWarpScan] += 1u;
+                        s.c[kStatSectors] += range_sectors(v, ls, rs);
+                    }
+                }
             }
         }
+    }
+}
+
+// Adds a thread's counters to the launch's device counters (one atomic per
+// warp and counter).
+__device__ __forceinline__ void flush_stats(const QStats &s, unsigned long long *out) {
+#pragma unroll
+    for (int c = 0; c < kStatCount; ++c) {
+        unsigned long long x = s.c[c];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + c, x);
     }
 }
 
@@ -362,10 +755,11 @@ template <bool ALIGNED, int QPT>
 __device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o, int64_t q0,
                                              int64_t q1) {
     const int64_t step = static_cast<int64_t>(blockDim.x) * QPT;
+    QStats s;
     for (int64_t base = q0; base < q1; base += step) {
         int2 qq[QPT];
         load_queries<QPT>(o, base, q1, qq);
-        answer_step<ALIGNED, QPT>(v, o, base, q1, qq);
+        answer_step<ALIGNED, QPT, false>(v, o, base, q1, qq, s);
     }
 }
 
