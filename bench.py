@@ -5,11 +5,13 @@ plain RMQ over n = 1e8 float32 values uniform in [0,1) (seed 1321) with
 q = 2^26 inclusive (l, r) queries, values and leftmost indices both returned.
 The headline step is one rmq_query over the uniform-length queries (lr=-1);
 the other length modes of the same configuration (lr=-2, lr=-3, fixed
-len 2^10) are timed the same way and reported under "modes". The block size
-of each mode is the fastest of a sweep over 2^10..2^16 (the workload's range)
-and 2^7..2^9 (short ranges are cheapest as cross-block queries over small
-blocks, whose coarse table stays in L2); "best_in_2^10..2^16" keeps the
-fastest inside the workload's range.
+len 2^10) are timed the same way and reported under "modes". Each mode's
+block size is the fastest of a sweep over every power of two in 2^10..2^16
+(the workload's range); the sweep also covers 2^7..2^9, reported apart as
+"best_below_2^10".
+
+Inputs are generated here with numpy (same seeds for both arms), so the
+reference arm never loads this package.
 
 value      -- RMQ/s of the device-resident step (inputs already in HBM),
               timed with CUDA events on the launching stream.
@@ -17,13 +19,21 @@ e2e        -- the same step through the C ABI with host buffers
               (rmq_query_host): the query kernel reads the pinned host queries
               and writes values + indices into pinned host memory over
               NVLink-C2C, all inside the timed region.
-roofline   -- algorithmic HBM bytes per launch (query read + result write +
-              one 32-byte sector per pre/suf lookup, 32 bytes per sector a
-              block scan touches) / kernel time, against the measured copy
-              bandwidth.
+roofline   -- algorithmic HBM bytes per launch / kernel time against the
+              measured copy bandwidth. The bytes are the query read and the
+              result write (16 B per query) plus 32 B per per-element entry and
+              per 32-byte sector of values the kernel must read, counted for
+              this query set by rmq_query_stats (the kernel's counting
+              instantiation). The small-table probes are L2-resident and
+              reported apart, as is the un-pruned 80 B/query figure.
 cpu_baseline -- the reference's CPU comparator HRMQ (restated in the
               oracle, hrmq_port.c) on this host's cores, on a bounded sample
               of the same queries.
+
+Further sections: the tie-heavy configuration (n = 2^27 integers in
+[0, 256), five fixed lengths), the CPU-runnable configuration (n = 1e6,
+q = 2^20, lr=-3, L2 flushed before every timed step), the batched ragged
+configuration and the differentiable one.
 
 `--impl reference` times that CPU path alone (rank 0) and prints its own line.
 """
@@ -31,6 +41,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -47,8 +58,13 @@ N_ELEMS = 10**8
 N_QUERIES = 1 << 26
 SEED = 1321
 MODES = [("lr=-1", -1), ("lr=-2", -2), ("lr=-3", -3), ("len=2^10", 1024)]
-BS_SWEEP = [1 << 7, 1 << 8, 1 << 9, 1 << 10, 1 << 12, 1 << 14, 1 << 16]
+BS_RANGE = [1 << k for k in range(10, 17)]       # the workload's block-size range
+BS_BELOW = [1 << 7, 1 << 8, 1 << 9]              # extra: short ranges over small blocks
+TIE_N = 1 << 27
+TIE_LENGTHS = [1, 32, 1 << 10, 1 << 16, 1 << 22]
 PUBLISHED_LR1 = 3.52e8  # RTXRMQ alg 5, RTX 6000 Ada (csv-to-plot/perf-RTX6000ADA-ALG5.csv:1586-1601)
+L2_NOTE = ("no flush: the per-step working set (values, index entries, queries, outputs; "
+           "2.9 GB at n=1e8) is larger than L2")
 
 
 def parse():
@@ -64,6 +80,8 @@ def parse():
     ap.add_argument("--bs", type=int, default=0, help="fixed block size (skips the sweep)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end step")
     ap.add_argument("--skip-plain", action="store_true", help="skip the plain modes (headline)")
+    ap.add_argument("--skip-tie", action="store_true", help="skip the tie-heavy configuration")
+    ap.add_argument("--skip-small", action="store_true", help="skip the n=1e6 configuration")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--batch-bs", type=int, default=0,
                     help="fixed block size for every bucket (skips the autotuner)")
@@ -72,7 +90,44 @@ def parse():
     ap.add_argument("--batch-q", type=int, default=1 << 26)
     ap.add_argument("--diff-rows", type=int, default=256)
     ap.add_argument("--diff-qpr", type=int, default=1 << 16)
+    ap.add_argument("--probe-gib", type=int, default=4,
+                    help="GiB of the layout-independent random-access probe's buffer")
     return ap.parse_args()
+
+
+# ---------------------------------------------------------------- inputs (numpy)
+
+def np_values_uniform(n: int, seed: int) -> np.ndarray:
+    """float32 uniform in [0, 1) with 24-bit resolution."""
+    return np.random.default_rng(seed).random(n, dtype=np.float32)
+
+
+def np_values_int(n: int, vrange: int, seed: int) -> np.ndarray:
+    """Integers uniform in [0, vrange) stored as float32 (tie-heavy)."""
+    return np.random.default_rng(seed).integers(0, vrange, n).astype(np.float32)
+
+
+def np_queries(q: int, n: int, lr: int, seed: int) -> np.ndarray:
+    """int32 [q, 2] inclusive queries with the reference's length modes
+    (src/rand.cuh:179-201): lr > 0 fixed length; -1 uniform in [1, n];
+    -2 / -3 round(lognormal(0.6 / 0.3 * ln n, 0.3)) clamped to [1, n];
+    l uniform in [0, n - len], r = l + len - 1."""
+    rng = np.random.default_rng(seed)
+    if lr > 0:
+        ln = np.full(q, min(lr, n), dtype=np.int64)
+    elif lr == -1:
+        ln = rng.integers(1, n + 1, q)
+    else:
+        mu = {-2: 0.6, -3: 0.3}[lr] * math.log(n)
+        ln = np.clip(np.rint(rng.lognormal(mu, 0.3, q)), 1, n).astype(np.int64)
+    l = np.minimum((rng.random(q) * (n - ln + 1)).astype(np.int64), n - ln)
+    return np.stack([l, l + ln - 1], axis=1).astype(np.int32)
+
+
+def query_seed(rank: int, lr: int) -> int:
+    """Seed of rank `rank`'s query set for length mode `lr` (replicas answer
+    different query sets)."""
+    return SEED + 1 + 1000 * rank + (0 if lr == -1 else 17 * abs(lr))
 
 
 # ---------------------------------------------------------------- helpers
@@ -139,42 +194,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.lines), "samples_under_load": n_load}
 
 
-def algorithmic_bytes(Q: np.ndarray, n: int, bs: int, out_bytes: int) -> tuple[float, dict]:
-    """HBM bytes the query kernel must move for this query set, following
-    the kernel's own decision per query (see query.cu)."""
-    l = Q[:, 0].astype(np.int64)
-    r = Q[:, 1].astype(np.int64)
-    lB, rB = l // bs, r // bs
-    cross = lB != rB
-    bstart = lB * bs
-    bend = np.minimum(bstart + bs, n) - 1
-    edge = (~cross) & ((l == bstart) | (r == bend))
-    scan = (~cross) & ~edge
-
-    def sectors(a, b):  # 32-byte sectors spanned by A[a..b]
-        return (b * 4) // 32 - (a * 4) // 32 + 1
-
-    per_q = 8 + out_bytes
-    # an edge query loads suf[l] when r ends its block and pre[r] when l
-    # starts it (both for a query over one whole block)
-    edge_sec = ((~cross) & (r == bend)).sum() + ((~cross) & (l == bstart)).sum()
-    total = per_q * len(Q) + 64.0 * cross.sum() + 32.0 * edge_sec
-    micro = bs >= 64  # the sub-block level exists for every bs >= 64
-    if micro:
-        # sub-block level: inside one 32-element micro-block a scan of its
-        # line; otherwise one sector each for the in-micro-block suffix at l
-        # and prefix at r, plus two micro-table entries when micro-blocks lie
-        # between
-        ls, rs = l[scan], r[scan]
-        ml, mr = ls // 32, rs // 32
-        one = ml == mr
-        sec = np.where(one, sectors(ls, rs), 2 + 2 * (mr - ml >= 2))
-    else:
-        sec = sectors(l[scan], r[scan])
-    total += 32.0 * sec.sum()
-    return float(total), {"cross_block": float(cross.mean()), "edge": float(edge.mean()),
-                          "same_block": float(scan.mean()), "sub_block_level": bool(micro),
-                          "mean_same_block_sectors": float(sec.mean()) if scan.any() else 0.0}
+def stats_bytes(st: dict, q: int, out_bytes: int = 8) -> dict:
+    """Algorithmic bytes of one query launch from the kernel's own counts
+    (rmq_query_stats): the query read and result write, plus one 32-byte
+    sector per per-element entry and per scanned sector of values (random
+    HBM); the small-table words are L2-resident and reported apart."""
+    hbm = q * (8 + out_bytes) + 32 * (st["entries"] + st["scan_sectors"])
+    valid = max(1, q - st["invalid"])
+    return {"alg_bytes": float(hbm), "alg_bytes_per_query": hbm / q,
+            "unpruned_alg_bytes": float(q * (8 + out_bytes + 64)),
+            "l2_table_words_per_query": st["table_words"] / valid,
+            "entries_per_query": st["entries"] / valid,
+            "entry_lookups_skipped": 1.0 - st["entries"] / (2.0 * valid),
+            "settled": {k: st[k] / valid for k in ("first_probe", "second_probe", "full",
+                                                   "micro_scan", "block_edge", "warp_scan")},
+            "scan_sectors_per_query": st["scan_sectors"] / valid}
 
 
 STEP_MIN = {}  # id(fn) -> fastest single step of the last time_steps(fn) call, ms
@@ -202,13 +236,39 @@ def time_steps(fn, steps, warmup, stream, barrier):
     return max_over_ranks(ev[0].elapsed_time(ev[steps]) / steps, dev)
 
 
+def time_steps_flushed(fn, steps, warmup, stream, barrier, flush_buf):
+    """As time_steps, for working sets that fit in L2: before every step a
+    write of `flush_buf` (larger than L2) evicts it, outside the timed
+    events."""
+    import torch
+    for _ in range(warmup):
+        flush_buf.zero_()
+        fn()
+    barrier()
+    torch.cuda.synchronize()
+    total, best = 0.0, float("inf")
+    for _ in range(steps):
+        flush_buf.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b)
+        total += t
+        best = min(best, t)
+    barrier()
+    from rtxrmq_gb300.replicas import max_over_ranks
+    dev = torch.cuda.current_device()
+    return max_over_ranks(total / steps, dev), max_over_ranks(best, dev)
+
+
 # ---------------------------------------------------------------- CPU side
 
 CPU_KIND = ("HRMQ restated (oracle/hrmq_port.c: balanced-parentheses RMQ of the reference's "
             "hrmq/RMQRMM64.cpp, ties leftmost), queries on all host threads")
 
-
-TRAFFIC_PROFILE = Path(__file__).resolve().parent / "profiles" / "query_kernel_plain_n1e8_q2e26_lr1.md"
+TRAFFIC_PROFILE = ROOT / "profiles" / "query_kernel_plain_n1e8_q2e26_lr1.md"
 
 
 def profiled_traffic(q):
@@ -222,6 +282,15 @@ def profiled_traffic(q):
     except OSError:
         pass
     return None
+
+
+def headline_config(n, q, lr):
+    default = n == N_ELEMS and q == N_QUERIES and lr == -1
+    label = "n=1e8 q=2^26 lr=-1" if default else f"n={n} q={q} lr={lr}"
+    return default, label, {
+        "workload": ("plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices" if default
+                     else f"plain RMQ {label}, values+indices"),
+        "n": n, "q": q, "lr": lr, "seed": SEED, "l2": L2_NOTE}
 
 
 def cpu_sample_rate(A, Q, target_s=12.0, nt=0):
@@ -250,16 +319,17 @@ def cpu_sample_rate(A, Q, target_s=12.0, nt=0):
 def run_reference(args, rank):
     """--impl reference: the reference's CPU path for this workload (HRMQ,
     restated in the oracle; the reference's compiled code cannot run on the
-    GPU host), rank 0 only, every step a bounded sample of the queries."""
+    GPU host), rank 0 only, every step a bounded sample of the queries.
+    Inputs come from the same numpy generators and seeds as the GPU arm;
+    this package is not imported."""
     if rank != 0:
         return
     import oracle
-    import rtxrmq_gb300 as R
     oracle.build(with_ref=False)
     nt = os.cpu_count() or 1
     n, q = args.n, args.q
-    A = R.gen_values_uniform(n, SEED)
-    Q = R.gen_queries(q, n, -1, SEED + 1)
+    A = np_values_uniform(n, SEED)
+    Q = np_queries(q, n, -1, query_seed(0, -1))
     t = time.perf_counter()
     h = oracle.HRMQ(A, strict=True, nt=nt)
     build_s = time.perf_counter() - t
@@ -278,12 +348,12 @@ def run_reference(args, rank):
         h.query(s, nt)
         times.append(time.perf_counter() - t)
     v = m * args.steps / sum(times)
-    line = {"metric": "RMQ/s n=1e8 q=2^26 lr=-1 (values+indices)", "value": v, "unit": "RMQ/s",
+    default, label, config = headline_config(n, q, -1)
+    line = {"metric": f"RMQ/s {label} (values+indices)", "value": v, "unit": "RMQ/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices",
-                       "n": n, "q": q, "lr": -1, "seed": SEED},
+            "config": config,
             "cpu_baseline": {"value": v, "unit": "RMQ/s", "cores": nt, "kind": "port",
                              "sample": f"{m} random queries per step from the {q}-query set; "
                                        f"{CPU_KIND}; construction {build_s:.2f} s"},
@@ -306,6 +376,213 @@ def graph_of(fn, stream):
         fn()
     torch.cuda.synchronize()
     return g
+
+
+def sweep_block_sizes(R, dA, dQ, out_v, out_i, bs_list, stream, barrier, q, world):
+    """RMQ/s of every block size in bs_list (3 timed steps each)."""
+    sweep = {}
+    for bs in bs_list:
+        if bs > dA.numel():
+            continue
+        with R.RMQIndex(dA, bs) as ix:
+            fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+            ms = time_steps(fn, 3, 1, stream, barrier)
+        sweep[bs] = q * world / (ms / 1e3)
+    return sweep
+
+
+def pick(sweep, lo, hi):
+    cand = [(k, v) for k, v in sweep.items() if lo <= k <= hi]
+    return max(cand, key=lambda kv: kv[1]) if cand else None
+
+
+def bench_plain_mode(R, dA, n, Q, out_v, out_i, args, stream, barrier, world, dev, rbuf):
+    """One length mode of the headline configuration: block-size sweep, the
+    timed steps at the best block size of the workload's range, the kernel's
+    own counts, and the two random-access probes."""
+    import torch
+
+    from rtxrmq_gb300.replicas import job_rate
+    q = len(Q)
+    dQ = torch.from_numpy(Q).to(dev)
+    if args.bs:
+        sweep, bs = {}, args.bs
+    else:
+        sweep = sweep_block_sizes(R, dA, dQ, out_v, out_i, BS_BELOW + BS_RANGE, stream, barrier,
+                                  q, world)
+        bs = pick(sweep, BS_RANGE[0], BS_RANGE[-1])[0]
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    ix = R.RMQIndex(dA, bs)
+    torch.cuda.synchronize()
+    construction_ms = (time.perf_counter() - t) * 1e3
+    fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+    ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
+    st = ix.query_stats(dQ)
+    acc = stats_bytes(st, q)
+    res = {"value": job_rate(q, world, ms), "ms_per_step": ms, "ms_per_step_min": STEP_MIN[id(fn)],
+           "bs": bs, "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
+           "best_below_2^10": pick(sweep, 1, BS_RANGE[0] - 1),
+           "construction_ms": construction_ms, "query_stats": st, "accounting": acc,
+           "achieved_gbs": acc["alg_bytes"] / (ms / 1e3) / 1e9,
+           "unpruned_achieved_gbs": acc["unpruned_alg_bytes"] / (ms / 1e3) / 1e9,
+           "info": ix.info()}
+    # random-access probes with the query kernel's grid and query stream:
+    # two random 8-B lookups per query into this index's prefix / suffix
+    # tables (rmq_probe_gather), and into a 4 GiB buffer (rmq_probe_random,
+    # independent of the index layout)
+    gfn = lambda: ix.probe_gather(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+    gms = time_steps(gfn, args.steps, args.warmup, stream, barrier)
+    rfn = lambda: R.probe_random(rbuf, dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+    rms = time_steps(rfn, args.steps, args.warmup, stream, barrier)
+    res["random_access"] = {
+        "probe_buffer_gib": rbuf.numel() * 8 / 2**30,
+        "probe_random_ms": rms, "probe_random_rmq_s": job_rate(q, world, rms),
+        "probe_random_gbs": q * 80 / (rms / 1e3) / 1e9,
+        "query_vs_probe_random": rms / ms,
+        "probe_gather_ms": gms, "query_vs_probe_gather": gms / ms,
+        "pattern": "per query: 8-B query read, two random 8-B loads, 8-B result write; "
+                   "probe_random over a 4 GiB buffer (hashed positions), probe_gather at "
+                   "suf[l] / pre[r] of this index"}
+    return res, ix, dQ
+
+
+def bench_e2e(ix, Q, dQ, out_v, out_i, args, stream, barrier, world, dev):
+    """rmq_query_host with pinned host buffers read and written in place,
+    and the host link's ceiling for the same bytes."""
+    import torch
+
+    from rtxrmq_gb300.replicas import job_rate
+    q = len(Q)
+    hQ = torch.from_numpy(Q).pin_memory()
+    hV = torch.empty(q, dtype=torch.float32).pin_memory()
+    hI = torch.empty(q, dtype=torch.int32).pin_memory()
+
+    def e2e():
+        ix.query_host(hQ, hV, hI)
+
+    e2e_ms = time_steps(e2e, args.steps, args.warmup, stream, barrier)
+    torch.cuda.synchronize()
+    dQc = torch.empty_like(dQ)
+    dR = torch.empty(2 * q, dtype=torch.int32, device=dev)
+    hR = torch.empty(2 * q, dtype=torch.int32).pin_memory()
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def link():
+        s_in.wait_stream(stream)
+        s_out.wait_stream(stream)
+        with torch.cuda.stream(s_in):
+            dQc.copy_(hQ, non_blocking=True)
+        with torch.cuda.stream(s_out):
+            hR.copy_(dR, non_blocking=True)
+        stream.wait_stream(s_in)
+        stream.wait_stream(s_out)
+
+    link_ms = time_steps(link, max(3, args.steps // 2), 2, stream, barrier)
+    del dQc, dR, hR
+    ix.query(dQ, out_val=out_v, out_idx=out_i)
+    torch.cuda.synchronize()
+    ok = (np.array_equal(hI.numpy(), out_i.cpu().numpy()) and
+          np.array_equal(hV.numpy().view(np.uint32), out_v.cpu().numpy().view(np.uint32)))
+    return {"value": job_rate(q, world, e2e_ms), "unit": "RMQ/s",
+            "h2d_bytes_per_step": int(Q.nbytes),
+            "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
+            "ms_per_step": e2e_ms,
+            "path": "rmq_query_host, pinned host buffers read and written in place",
+            "matches_device_path": bool(ok),
+            "link_ceiling": {"ms_per_step": link_ms, "rmq_s": job_rate(q, world, link_ms),
+                             "gbs_per_direction": Q.nbytes / (link_ms / 1e3) / 1e9,
+                             "frac": link_ms / e2e_ms,
+                             "how": "the step's query bytes in and result bytes out copied "
+                                    "concurrently (pinned, two streams)"}}
+
+
+def bench_energy(fn, ms, q, local):
+    import torch
+
+    from rtxrmq_gb300.power import PowerSampler
+    reps_e = max(1, int(1500.0 / max(ms, 1e-3)))
+    torch.cuda.synchronize()
+    with PowerSampler(local, sample_ms=50) as ps:
+        for _ in range(reps_e):
+            fn()
+        torch.cuda.synchronize()
+    if ps.available and ps.energy_joules:
+        return {"rmq_per_joule": q * reps_e / ps.energy_joules, "avg_watts": ps.avg_watts,
+                "seconds": ps.seconds, "reps": reps_e, "source": "NVML board power, 50 ms samples",
+                "reference": "RTXRMQ on RTX 6000 Ada: 1.20e6 RMQ/J (2^26 x 512 queries / "
+                             "28625.93 J, scripts/plot_rmq_per_joule.py:69)"}
+    return {"unavailable": f"NVML status {ps.status}"}
+
+
+def bench_tie_heavy(R, args, stream, barrier, world, rank, dev):
+    """Tie-heavy configuration: n = 2^27 floats holding integers uniform in
+    [0, 256), q = 2^26 queries of each fixed length; bs swept over the
+    workload's range (2^10..2^16) per length. Bit-exactness at this size is
+    asserted by tests/test_gpu_fullscale.py."""
+    import torch
+
+    from rtxrmq_gb300.replicas import job_rate
+    n, q = TIE_N, args.q
+    dA = torch.from_numpy(np_values_int(n, 256, SEED + 3)).to(dev)
+    out_v = torch.empty(q, dtype=torch.float32, device=dev)
+    out_i = torch.empty(q, dtype=torch.int32, device=dev)
+    res = {"workload": "n=2^27 float32 integers U{0..255}, q=2^26 per fixed length, "
+                       "values+indices", "l2": L2_NOTE}
+    for length in TIE_LENGTHS:
+        Q = np_queries(q, n, length, query_seed(rank, length) + 5)
+        dQ = torch.from_numpy(Q).to(dev)
+        sweep = sweep_block_sizes(R, dA, dQ, out_v, out_i, BS_RANGE, stream, barrier, q, world)
+        bs = pick(sweep, BS_RANGE[0], BS_RANGE[-1])[0]
+        with R.RMQIndex(dA, bs) as ix:
+            fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+            ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
+            st = ix.query_stats(dQ)
+        acc = stats_bytes(st, q)
+        res[f"len={length}"] = {"rmq_s": job_rate(q, world, ms), "ms_per_step": ms, "bs": bs,
+                                "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
+                                "settled": acc["settled"],
+                                "alg_bytes_per_query": acc["alg_bytes_per_query"],
+                                "achieved_gbs": acc["alg_bytes"] / (ms / 1e3) / 1e9}
+        del dQ
+    del dA, out_v, out_i
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_small(R, args, stream, barrier, world, rank, dev):
+    """CPU-runnable configuration: n = 1e6 U[0,1), q = 2^20, lr=-3. Its
+    working set fits in L2, so L2 is flushed (a 512 MB write) before every
+    timed step; bs swept over 2^7..2^16."""
+    import torch
+
+    from rtxrmq_gb300.replicas import job_rate
+    n, q = 10**6, 1 << 20
+    dA = torch.from_numpy(np_values_uniform(n, SEED)).to(dev)
+    Q = np_queries(q, n, -3, query_seed(rank, -3))
+    dQ = torch.from_numpy(Q).to(dev)
+    out_v = torch.empty(q, dtype=torch.float32, device=dev)
+    out_i = torch.empty(q, dtype=torch.int32, device=dev)
+    flush = torch.empty(1 << 27, dtype=torch.float32, device=dev)
+    sweep = {}
+    for bs in BS_BELOW + BS_RANGE:
+        with R.RMQIndex(dA, bs) as ix:
+            fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+            ms, _ = time_steps_flushed(fn, 5, 1, stream, barrier, flush)
+        sweep[bs] = job_rate(q, world, ms)
+    bs = max(sweep.items(), key=lambda kv: kv[1])[0]
+    with R.RMQIndex(dA, bs) as ix:
+        fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+        ms, best = time_steps_flushed(fn, args.steps, args.warmup, stream, barrier, flush)
+        st = ix.query_stats(dQ)
+    acc = stats_bytes(st, q)
+    del dA, dQ, out_v, out_i, flush
+    torch.cuda.empty_cache()
+    return {"workload": "n=1e6 U[0,1), q=2^20, lr=-3 (lognormal 0.3 ln n), values+indices",
+            "l2": "flushed (512 MB write) before every timed step: the working set fits in L2",
+            "rmq_s": job_rate(q, world, ms), "ms_per_step": ms, "ms_per_step_min": best,
+            "bs": bs, "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
+            "settled": acc["settled"], "alg_bytes_per_query": acc["alg_bytes_per_query"]}
 
 
 def bench_batched(args, dev, stream, barrier):
@@ -363,11 +640,11 @@ def bench_batched(args, dev, stream, barrier):
                 "build_only_ms": bms, "query_only_ms": qms,
                 "query_only_rmq_s": job_rate(q, nr, qms),
                 # algorithmic bytes of one step: the build reads each value once and
-                # writes its prefix / suffix entries (4 + 16 B per element), each
-                # query reads its pair and two random 32-B sectors and writes 8 B
-                # (80 B; table probes excluded); against the graph-launched step
-                "alg_bytes_per_step": int(w.lengths.sum()) * 20 + q * 80,
-                "alg_gbs": (int(w.lengths.sum()) * 20 + q * 80) / (gms / 1e3) / 1e9,
+                # writes its prefix / suffix entries (4 + 16 B per element); each
+                # query reads its pair and writes 8 B, plus at most two random 32-B
+                # entry sectors (the un-pruned bound); against the graph-launched step
+                "alg_bytes_per_step_unpruned": int(w.lengths.sum()) * 20 + q * 80,
+                "alg_gbs_unpruned": (int(w.lengths.sum()) * 20 + q * 80) / (gms / 1e3) / 1e9,
                 "launches_per_step": {"batched": 1, "per_array": "one build + level + query "
                                       "launch sequence per array"}})
     del dV, dQ, ov, oi
@@ -449,7 +726,6 @@ def main():
     import torch.distributed as dist
 
     import rtxrmq_gb300 as R
-    from rtxrmq_gb300.replicas import job_rate, rank_seed
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -463,149 +739,58 @@ def main():
     n, q = args.n, args.q
     hbm_peak, peak_kind = peaks()
 
-    A = R.gen_values_uniform(n, SEED)
-    dA = torch.from_numpy(A).to(dev)
     modes = MODES if args.modes == "all" else [(f"lr={m}", int(m)) for m in args.modes.split(",")]
     if args.skip_plain:
         modes = []
-    out_v = torch.empty(q, dtype=torch.float32, device=dev)
-    out_i = torch.empty(q, dtype=torch.int32, device=dev)
 
     results = {}
     headline = None
+    ref_nb = {}
+    tie = small = batched = autograd = None
+    A = None
     sampler = ClockSampler(local)
     with sampler:
-        for name, lr in modes:
-            # replicas: each rank answers its own query set (seeded by rank)
-            Q = R.gen_queries(q, n, lr, rank_seed(SEED, rank, lr))
-            dQ = torch.from_numpy(Q).to(dev)
-            sweep = {}
-            best = None
-            for bs in ([args.bs] if args.bs else BS_SWEEP):
-                ix = R.RMQIndex(dA, bs)
-                fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
-                ms = time_steps(fn, 3, 1, stream, barrier)
-                sweep[bs] = q / (ms / 1e3)
-                if best is None or ms < best[1]:
-                    best = (bs, ms)
-                ix.close()
-            bs = best[0]
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            ix = R.RMQIndex(dA, bs)
-            torch.cuda.synchronize()
-            construction_ms = (time.perf_counter() - t) * 1e3
-            fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
-            ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
-            alg_bytes, mix = algorithmic_bytes(Q, n, bs, 8)
-            res = {"value": job_rate(q, world, ms), "ms_per_step": ms,
-                   "ms_per_step_min": STEP_MIN[id(fn)], "bs": bs,
-                   "bs_sweep_rmq_s": {str(k): v for k, v in sweep.items()},
-                   "best_in_2^10..2^16": max(((k, v) for k, v in sweep.items() if k >= 1 << 10),
-                                             key=lambda kv: kv[1], default=None),
-                   "construction_ms": construction_ms, "mix": mix,
-                   "alg_bytes_per_step": alg_bytes,
-                   "achieved_gbs": alg_bytes / (ms / 1e3) / 1e9,
-                   "info": ix.info()}
-            if lr == -1 and not args.no_e2e:
-                # end to end through the C ABI with host buffers: rmq_query_host
-                # reads the pinned queries and writes the pinned results in
-                # place over NVLink-C2C inside the timed region
-                hQ = torch.from_numpy(Q).pin_memory()
-                hV = torch.empty(q, dtype=torch.float32).pin_memory()
-                hI = torch.empty(q, dtype=torch.int32).pin_memory()
-
-                def e2e():
-                    ix.query_host(hQ, hV, hI)
-
-                e2e_ms = time_steps(e2e, args.steps, args.warmup, stream, barrier)
-                torch.cuda.synchronize()
-                # the host link's ceiling for this traffic: the step's bytes in
-                # and out copied at the same time on two streams (copy engines;
-                # kernel loads and stores over NVLink-C2C reach the same rate)
-                dQc = torch.empty_like(dQ)
-                dR = torch.empty(2 * q, dtype=torch.int32, device=dev)
-                hR = torch.empty(2 * q, dtype=torch.int32).pin_memory()
-                s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
-
-                def link():
-                    s_in.wait_stream(stream)
-                    s_out.wait_stream(stream)
-                    with torch.cuda.stream(s_in):
-                        dQc.copy_(hQ, non_blocking=True)
-                    with torch.cuda.stream(s_out):
-                        hR.copy_(dR, non_blocking=True)
-                    stream.wait_stream(s_in)
-                    stream.wait_stream(s_out)
-
-                link_ms = time_steps(link, max(3, args.steps // 2), 2, stream, barrier)
-                del dQc, dR, hR
-                ix.query(dQ, out_val=out_v, out_idx=out_i)
-                torch.cuda.synchronize()
-                ok = (np.array_equal(hI.numpy(), out_i.cpu().numpy()) and
-                      np.array_equal(hV.numpy().view(np.uint32), out_v.cpu().numpy().view(np.uint32)))
-                res["e2e"] = {"value": job_rate(q, world, e2e_ms), "unit": "RMQ/s",
-                              "h2d_bytes_per_step": int(Q.nbytes),
-                              "d2h_bytes_per_step": int(hV.numel() * 4 + hI.numel() * 4),
-                              "ms_per_step": e2e_ms, "path": "rmq_query_host, pinned host buffers read and written in place",
-                              "matches_device_path": bool(ok),
-                              "link_ceiling": {"ms_per_step": link_ms,
-                                               "rmq_s": job_rate(q, world, link_ms),
-                                               "gbs_per_direction": Q.nbytes / (link_ms / 1e3) / 1e9,
-                                               "frac": link_ms / e2e_ms,
-                                               "how": "the step's query bytes in and result bytes out "
-                                                      "copied concurrently (pinned, two streams)"}}
-                del hQ, hV, hI
-            # random-access ceiling on this index and this mode's queries:
-            # rmq_probe_gather has the query kernel's grid, query stream and
-            # stores but only two random lookups (suf[l], pre[r]) per query
-            gfn = lambda: ix.probe_gather(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
-            gms = time_steps(gfn, args.steps, args.warmup, stream, barrier)
-            res["random_access"] = {
-                "ceiling_rmq_s": job_rate(q, world, gms), "ceiling_ms_per_step": gms,
-                "frac": gms / ms, "kernel": "gather_kernel (rmq_probe_gather)",
-                "pattern": "per query: 8-B query read, two random 8-B lookups (suf[l], pre[r]) "
-                           "in the 0.8 GB prefix / suffix tables, 8-B result write"}
-            if lr == -1:
-                headline = (name, lr, Q, bs)
-                # energy: NVML board power over ~1.5 s of headline steps (outside
-                # the timed region), as the reference's power CSVs
-                # (scripts/plot_rmq_per_joule.py: q * reps / joules)
-                from rtxrmq_gb300.power import PowerSampler
-                reps_e = max(1, int(1500.0 / max(ms, 1e-3)))
-                torch.cuda.synchronize()
-                with PowerSampler(local, sample_ms=50) as ps:
-                    for _ in range(reps_e):
-                        fn()
-                    torch.cuda.synchronize()
-                if ps.available and ps.energy_joules:
-                    res["energy"] = {"rmq_per_joule": q * reps_e / ps.energy_joules,
-                                     "avg_watts": ps.avg_watts, "seconds": ps.seconds,
-                                     "reps": reps_e, "source": "NVML board power, 50 ms samples",
-                                     "reference": "RTXRMQ on RTX 6000 Ada: 1.20e6 RMQ/J "
-                                                  "(2^26 x 512 queries / 28625.93 J, "
-                                                  "scripts/plot_rmq_per_joule.py:69)"}
-                else:
-                    res["energy"] = {"unavailable": f"NVML status {ps.status}"}
-            ix.close()
-            results[name] = res
-            del dQ
-        # the reference's own block sizes: its benchmark scripts pass --nb 512
-        # (lr=-1, -2) and --nb 8192 (lr=-3), bs = n / nb
-        # (scripts/perf-fulltest.sh:49-58, src/tools.h:129-132)
-        ref_nb = {}
-        if modes and not args.bs:
-            for name, lr, nb in (("lr=-1", -1, 512), ("lr=-2", -2, 512), ("lr=-3", -3, 8192)):
-                bs = R.bs_from_nb(n, nb)
-                Q = R.gen_queries(q, n, lr, rank_seed(SEED, rank, lr))
-                dQ = torch.from_numpy(Q).to(dev)
-                with R.RMQIndex(dA, bs) as ix:
+        if modes:
+            A = np_values_uniform(n, SEED)
+            dA = torch.from_numpy(A).to(dev)
+            out_v = torch.empty(q, dtype=torch.float32, device=dev)
+            out_i = torch.empty(q, dtype=torch.int32, device=dev)
+            # words for the layout-independent random-access probe (4 GiB)
+            rbuf = torch.arange(args.probe_gib << 27, dtype=torch.int64, device=dev)
+            for name, lr in modes:
+                Q = np_queries(q, n, lr, query_seed(rank, lr))
+                res, ix, dQ = bench_plain_mode(R, dA, n, Q, out_v, out_i, args, stream, barrier,
+                                               world, dev, rbuf)
+                if lr == -1:
+                    headline = (name, lr, Q)
+                    if not args.no_e2e:
+                        res["e2e"] = bench_e2e(ix, Q, dQ, out_v, out_i, args, stream, barrier,
+                                               world, dev)
                     fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
-                    ms = time_steps(fn, max(3, args.steps // 2), 2, stream, barrier)
-                ref_nb[name] = {"nb": nb, "bs": bs, "rmq_s": job_rate(q, world, ms), "ms_per_step": ms}
+                    res["energy"] = bench_energy(fn, res["ms_per_step"], q, local)
+                ix.close()
+                results[name] = res
                 del dQ
-        del dA
-        torch.cuda.empty_cache()
+            del rbuf
+            # the reference's own block sizes: its benchmark scripts pass --nb 512
+            # (lr=-1, -2) and --nb 8192 (lr=-3), bs = n / nb
+            # (scripts/perf-fulltest.sh:49-58, src/tools.h:129-132)
+            if not args.bs and args.modes == "all":
+                for name, lr, nb in (("lr=-1", -1, 512), ("lr=-2", -2, 512), ("lr=-3", -3, 8192)):
+                    bs = R.bs_from_nb(n, nb)
+                    dQ = torch.from_numpy(np_queries(q, n, lr, query_seed(rank, lr))).to(dev)
+                    with R.RMQIndex(dA, bs) as ix:
+                        fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+                        ms = time_steps(fn, max(3, args.steps // 2), 2, stream, barrier)
+                    ref_nb[name] = {"nb": nb, "bs": bs, "rmq_s": q * world / (ms / 1e3),
+                                    "ms_per_step": ms}
+                    del dQ
+            del dA, out_v, out_i
+            torch.cuda.empty_cache()
+        if not args.skip_tie and args.modes == "all":
+            tie = bench_tie_heavy(R, args, stream, barrier, world, rank, dev)
+        if not args.skip_small and args.modes == "all":
+            small = bench_small(R, args, stream, barrier, world, rank, dev)
         batched = None if args.skip_batched else bench_batched(args, dev, stream, barrier)
         autograd = None if args.skip_autograd else bench_autograd(args, dev, stream, barrier)
     clocks = sampler.summary()
@@ -614,19 +799,17 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return
-    if not results:  # a run of the batched / autograd sections only
-        print(json.dumps({"metric": "batched / differentiable sections only", "value": None,
-                          "clocks": clocks, "batched": batched, "autograd": autograd}), flush=True)
+    if not results:  # a run of the other sections only
+        print(json.dumps({"metric": "sections other than the headline only", "value": None,
+                          "clocks": clocks, "tie_heavy": tie, "small_config": small,
+                          "batched": batched, "autograd": autograd}), flush=True)
         if world > 1:
             dist.destroy_process_group()
         return
-    name, lr, Q, bs = headline if headline else (modes[0][0], modes[0][1], None, None)
+    name, lr, Q = headline if headline else (modes[0][0], modes[0][1], None)
     h = results[name]
-    bs = h["bs"]
     achieved = h["achieved_gbs"]
-    # the headline workload, or (a run of other modes / sizes) the one measured
-    default_run = lr == -1 and n == N_ELEMS and q == N_QUERIES
-    label = "n=1e8 q=2^26 lr=-1" if default_run else f"n={n} q={q} {name}"
+    default, label, config = headline_config(n, q, lr)
     line = {
         "metric": f"RMQ/s {label} (values+indices)",
         "value": h["value"], "unit": "RMQ/s", "n_gpus": world, "steps": args.steps,
@@ -634,33 +817,38 @@ def main():
         "ms_per_step_min": h["ms_per_step_min"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": h["value"] / PUBLISHED_LR1,
         "vs_baseline_ref": "RTXRMQ (alg 5) on RTX 6000 Ada, 3.52e8 RMQ/s, n=1e8 q=2^26 lr=-1",
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": ("plain RMQ n=1e8 q=2^26 lr=-1 (uniform length), values+indices"
-                                if default_run else f"plain RMQ {label}, values+indices"),
-                   "n": n, "q": q, "lr": lr, "bs": bs, "seed": SEED,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "no flush: per-step working set (2.9 GB: values, pre/suf, queries, "
-                         "outputs) is larger than L2"},
+        "dtype": "f32", "data": "synthetic (numpy generators, seed 1321)",
+        "config": config,
+        "bs": h["bs"],
+        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         "e2e": h.get("e2e"),
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
                      # DRAM bytes captured by ncu on the headline workload only
-                     "traffic": profiled_traffic(q) if default_run else None,
-                     "traffic_source": TRAFFIC_PROFILE.name if default_run else None,
+                     "traffic": profiled_traffic(q) if default else None,
+                     "traffic_source": TRAFFIC_PROFILE.name if default else None,
                      "peak_kind": f"{peak_kind} copy bandwidth",
-                     "kernel": "query_kernel", "alg_bytes_per_launch": h["alg_bytes_per_step"]},
+                     "kernel": "query_kernel",
+                     "alg_bytes_per_launch": h["accounting"]["alg_bytes"],
+                     "alg_bytes_basis": "16 B per query (query read, value + index write) + 32 B "
+                                        "per per-element entry read and per 32-B sector of values "
+                                        "scanned, counted by rmq_query_stats on this query set",
+                     "l2_table_words_per_query": h["accounting"]["l2_table_words_per_query"],
+                     "unpruned_alg_bytes_per_launch": h["accounting"]["unpruned_alg_bytes"],
+                     "unpruned_achieved": h["unpruned_achieved_gbs"],
+                     "unpruned_frac": h["unpruned_achieved_gbs"] / hbm_peak},
         "random_access_roofline": h.get("random_access"),
-        "random_access_frac_by_mode": {k: v["random_access"]["frac"] for k, v in results.items()
-                                       if "random_access" in v},
         "clocks": clocks,
         "modes": {k: {kk: vv for kk, vv in v.items() if kk not in ("info",)} for k, v in results.items()},
         "modes_reference_nb": ref_nb,
         "energy": h.get("energy"),
+        "tie_heavy": tie,
+        "small_config": small,
         "batched": batched,
         "autograd": autograd,
     }
-    if not args.no_cpu and world == 1:
+    if not args.no_cpu and world == 1 and A is not None and Q is not None:
         v, meta = cpu_sample_rate(A, Q)
         line["cpu_baseline"] = {"value": v, "unit": "RMQ/s", "cores": meta["cores"], "kind": "port",
                                 "sample": meta["sample"] + "; " + CPU_KIND}

@@ -242,14 +242,27 @@ def test_bench_and_entry_compile():
         py_compile.compile(str(root / f), doraise=True)
 
 
-def test_bench_reference_arm(native, oracle_lib):
+def _bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    return bench
+
+
+def test_bench_reference_arm(oracle_lib):
     """`bench.py --impl reference` (the reference's CPU comparator, HRMQ
-    restated) prints one JSON line with the contract's keys."""
+    restated) prints one JSON line with the contract's keys and the GPU
+    arm's config, and never imports this package (its inputs come from
+    bench.py's own numpy generators)."""
     import json
     import subprocess
     import sys
     root = Path(__file__).resolve().parent.parent
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n", "1000000",
+    code = ("import runpy, sys; sys.argv = ['bench.py'] + sys.argv[1:]; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "assert not [m for m in sys.modules if m.startswith('rtxrmq_gb300')], 'package imported'")
+    r = subprocess.run([sys.executable, "-c", code, "--impl", "reference", "--n", "1000000",
                         "--q", "100000", "--steps", "3", "--warmup", "3"],
                        cwd=root, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -257,6 +270,50 @@ def test_bench_reference_arm(native, oracle_lib):
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "RMQ/s"
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["steps"] == 3
+    bench = _bench_module()
+    assert line["config"] == bench.headline_config(1000000, 100000, -1)[2]
+    assert line["metric"] == "RMQ/s n=1000000 q=100000 lr=-1 (values+indices)"
+
+
+def test_bench_query_generators():
+    """bench.py's numpy inputs: queries in range with the reference's length
+    modes (fixed, uniform, lognormal 0.6 / 0.3 ln n), deterministic in the
+    seed; values in [0, 1) and tie-heavy integers."""
+    import math
+    bench = _bench_module()
+    n, q = 10**6, 200_000
+    for lr in (-1, -2, -3, 1, 1024, n):
+        Q = bench.np_queries(q, n, lr, 7)
+        assert Q.dtype == np.int32 and Q.shape == (q, 2)
+        ln = Q[:, 1].astype(np.int64) - Q[:, 0] + 1
+        assert (Q[:, 0] >= 0).all() and (ln >= 1).all() and (Q[:, 1] < n).all()
+        if lr > 0:
+            assert (ln == lr).all()
+        elif lr == -1:
+            assert abs(ln.mean() / (n / 2) - 1) < 0.01
+        else:
+            mu = {-2: 0.6, -3: 0.3}[lr] * math.log(n)
+            assert abs(np.log(ln).mean() - mu) < 0.01
+        assert np.array_equal(Q, bench.np_queries(q, n, lr, 7))
+    A = bench.np_values_uniform(n, 1)
+    assert A.dtype == np.float32 and A.min() >= 0 and A.max() < 1
+    T = bench.np_values_int(n, 256, 1)
+    assert set(np.unique(T)) == set(float(x) for x in range(256))
+
+
+def test_bench_accounting():
+    """Algorithmic bytes from the kernel's counts: 16 B per query plus 32 B
+    per per-element entry and per scanned sector; skipped lookups against
+    the un-pruned two per query."""
+    bench = _bench_module()
+    st = {"first_probe": 90, "second_probe": 6, "full": 2, "micro_scan": 0, "block_edge": 0,
+          "warp_scan": 1, "entries": 10, "table_words": 300, "scan_sectors": 3, "invalid": 1}
+    acc = bench.stats_bytes(st, 100)
+    assert acc["alg_bytes"] == 100 * 16 + 32 * 13
+    assert acc["unpruned_alg_bytes"] == 100 * 80
+    assert acc["entries_per_query"] == 10 / 99
+    assert abs(acc["entry_lookups_skipped"] - (1 - 10 / 198)) < 1e-12
+    assert abs(sum(acc["settled"].values()) - 1.0) < 1e-12
 
 
 def test_normal_build_reports_not_checked(native):
@@ -279,39 +336,6 @@ def test_batch_argument_types(native):
         B._queries(torch.zeros((4, 2), dtype=torch.int64))
     with pytest.raises(TypeError):
         B._queries(torch.zeros((4, 3), dtype=torch.int32))
-
-
-def test_algorithmic_bytes_per_query(native):
-    """bench.py's algorithmic bytes equal a per-query count that follows the
-    query kernel's decisions one query at a time."""
-    import importlib.util
-
-    import rtxrmq_gb300 as R
-    spec = importlib.util.spec_from_file_location("bench", ROOT / "bench.py")
-    bench = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(bench)
-
-    def one(l, r, n, bs):
-        b = 16  # query + value and index
-        lb, rb = l // bs, r // bs
-        if lb != rb:
-            return b + 64
-        bstart, bend = lb * bs, min(lb * bs + bs, n) - 1
-        if l == bstart or r == bend:
-            return b + 32 * ((r == bend) + (l == bstart))
-        if bs >= 64:
-            if l // 32 == r // 32:
-                return b + 32 * ((4 * r) // 32 - (4 * l) // 32 + 1)
-            return b + 64 + (64 if r // 32 - l // 32 >= 2 else 0)
-        return b + 32 * ((4 * r) // 32 - (4 * l) // 32 + 1)
-
-    n = 5000
-    Q = np.concatenate([R.gen_queries(700, n, L, 3 + k)
-                        for k, L in enumerate((-1, -2, -3, 1, 31, 64, 1000))])
-    Q = np.concatenate([Q, np.array([[0, 99], [100, 199], [0, n - 1], [4900, 4999]], np.int32)])
-    for bs in (1, 7, 32, 50, 64, 100, 1024, n):
-        total, _ = bench.algorithmic_bytes(Q, n, bs, 8)
-        assert total == sum(one(int(l), int(r), n, bs) for l, r in Q), bs
 
 
 def test_random_parity_cases_are_valid(native):
