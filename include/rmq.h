@@ -167,8 +167,9 @@ int rmq_query_host(const rmq_handle_t *h, const int32_t *h_queries, int64_t q,
  * queries are answered from it; the caller passes inputs and outputs as for
  * rmq_build + rmq_query, with the same results. Sizes whose index does not
  * fit are rejected with RMQ_EINVAL (any n <= 2^20 fits for bs >= 16).
- * The first call on a device looks up the array's device address (set-up),
- * so make that first call before any stream capture. All calls share the
+ * The first call on a device, and the first after the device's context was
+ * reset (cudaDeviceReset), looks up the array's device address (set-up),
+ * so make that call before any stream capture. All calls share the
  * array: calls whose work overlaps on the GPU race.
  */
 #define RMQ_NOALLOC_SCRATCH_BYTES (32u << 20)

@@ -12,14 +12,18 @@
 // The array is a file-scope __device__ variable of kNoallocScratchBytes, so
 // every GPU that loads this library holds it until the process exits. In
 // host code its name is only a host-side stand-in, never a device address:
-// the device address comes from cudaGetSymbolAddress, called once per device
-// with that device current (first call of rmq_query_noalloc on the device).
+// the device address comes from cudaGetSymbolAddress, called with that
+// device current on the first call of rmq_query_noalloc on the device and
+// again whenever the device's context has changed since (a device reset
+// ends the context, and the next one may place the array elsewhere).
 // All calls share the array and it keeps the last call's contents; the
 // counter is cleared by every call and everything else is rewritten before
 // it is read. Calls whose work overlaps on the GPU (different streams, or
 // different host threads) race on the array.
 #include <cstring>
 #include <mutex>
+
+#include <cuda.h>  // driver types only; the driver is reached through the runtime
 
 #include "../../include/rmq.h"
 #include "engine.h"
@@ -34,20 +38,55 @@ constexpr size_t kNoallocScratchBytes = static_cast<size_t>(RMQ_NOALLOC_SCRATCH_
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_noalloc_ctx[kMaxDevices] = {0};
+
+// Unique id of the calling thread's current context (cuCtxGetId), 0 when
+// there is none or the driver cannot tell. Context handles may be reused
+// after a reset; the ids are not.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static std::once_flag once;
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult st;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &st) ==
+                cudaSuccess && st == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &st) ==
+                cudaSuccess && st == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+        cudaGetLastError();
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c ||
+        get_id(c, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 // Device address of the scratch array on the current device (set-up on the
-// first call per device).
+// first call per device, repeated when the context is not the one the
+// address was taken in, or cannot be identified).
 int scratch_address(int device, void **out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_noalloc_ptr[device] || ctx == 0 || ctx != g_noalloc_ctx[device]) {
         void *p = nullptr;
         cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (err != cudaSuccess || !p) {
             cudaGetLastError();
+            g_noalloc_ptr[device] = nullptr;
             return set_error(RMQ_ECUDA, "rmq_query_noalloc: cudaGetSymbolAddress failed: %s",
                              cudaGetErrorString(err));
         }
         g_noalloc_ptr[device] = p;
+        // taken after the lookup, which makes the device's context current
+        g_noalloc_ctx[device] = current_context_id();
     }
     *out = g_noalloc_ptr[device];
     return RMQ_OK;

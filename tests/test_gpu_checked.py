@@ -86,6 +86,20 @@ for n in (1, 33, 300, 5000, 100_000, 300_001):
         assert rc == 0, rc
         eq(ni.cpu().numpy(), ei, "noalloc")
 
+# the no-allocation entry point on an index that fits its scratch only
+# without the sub-block level (the plain-index fallback)
+n = 1 << 20
+A = R.gen_values_int(n, 1000, 21)
+Q = R.gen_queries(50_000, n, -2, 22)
+ei = oracle.base_idx(A, Q)
+dA = torch.from_numpy(A).to(dev)
+nv = torch.empty(len(Q), device=dev); ni = torch.empty(len(Q), dtype=torch.int32, device=dev)
+rc = L.rmq_query_noalloc(dA.data_ptr(), n, 64, torch.from_numpy(Q).to(dev).data_ptr(), len(Q),
+                         nv.data_ptr(), ni.data_ptr(), None)
+assert rc == 0, rc
+eq(ni.cpu().numpy(), ei, "noalloc plain fallback")
+ran += 1
+
 # key modes
 A = rng.integers(-2**31, 2**31 - 1, 20000, dtype=np.int64).astype(np.int32)
 Q = R.gen_queries(20000, len(A), -3, 4)

@@ -43,6 +43,10 @@ def test_noalloc_matches_allocating_path(cuda, native):
     cases = [
         (1_000_000, 1024, -3, 11),  # first call: sub-block level, short ranges
         (777_777, 1000, -1, 12),    # second call: smaller array, other block size
+        # third call: the index fits the scratch only without the sub-block
+        # level (4 x 8 MiB of per-element entries alone fill it), so the
+        # entry point plans, places and answers from the plain index
+        (1 << 20, 64, -2, 13),
     ]
     for n, bs, lr, seed in cases:
         A = R.gen_values_int(n, 1000, seed)  # many ties
