@@ -25,7 +25,17 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref.so"
-REF_TREE = Path(os.environ.get("RTXRMQ_REFERENCE", "/root/reference"))
+# Where the build recipe below reads the reference's sources: the tree named
+# by RTXRMQ_REFERENCE, else the development container's mount point. Only
+# this recipe reads it; no other code of the project does.
+_DEV_REFERENCE_MOUNT = "/root/reference"
+
+
+def reference_tree() -> Path | None:
+    """The reference tree to compile oracle/_ref from, or None when absent."""
+    env = os.environ.get("RTXRMQ_REFERENCE")
+    t = Path(env) if env else Path(_DEV_REFERENCE_MOUNT)
+    return t if (t / "hrmq" / "RMQRMM64.cpp").exists() else None
 
 _vp, _i64, _i32 = C.c_void_p, C.c_int64, C.c_int
 _lib = None
@@ -33,14 +43,19 @@ _ref = None
 
 
 def build(with_ref: bool | None = None) -> None:
-    """Compile liboracle.so, and _ref/libref.so when the reference tree exists."""
+    """Compile liboracle.so; with_ref=None also compiles _ref/libref.so when
+    the reference tree is present, True requires it."""
     targets = ["all"]
+    ref = reference_tree()
+    if with_ref and ref is None:
+        raise FileNotFoundError("the reference tree was not found: set RTXRMQ_REFERENCE to it")
     if with_ref is None:
-        with_ref = (REF_TREE / "hrmq" / "RMQRMM64.cpp").exists()
+        with_ref = ref is not None
+    args = ["make", "-s", "-C", str(HERE)]
     if with_ref:
         targets.append("ref")
-    r = subprocess.run(["make", "-s", "-C", str(HERE), f"REF={REF_TREE}", *targets],
-                       capture_output=True, text=True)
+        args.append(f"REF={ref}")
+    r = subprocess.run([*args, *targets], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
 
