@@ -49,31 +49,34 @@ struct Args {
 
 void usage() {
     std::fprintf(stderr,
-                 "run as ./rtxrmq <n> <q> <lr> <alg>\n\n"
-                 "n   = num elements\n"
-                 "q   = num RMQ querys\n"
-                 "lr  = length of range; min 1, max n\n"
-                 "  >0 -> value\n"
-                 "  -1 -> uniform distribution (large values)\n"
-                 "  -2 -> lognormal distribution (medium values)\n"
-                 "  -3 -> lognormal distribution (small values)\n"
-                 "  -4, -5 -> lognormal around n/2^8, n/2^15\n"
-                 "alg = algorithm\n"
-                 "   2 -> %s\n"
-                 "   5 -> %s (RTXRMQ block decomposition, GB300 CUDA engine)\n"
-                 "   102, 105 -> algs 2 5 returning indices\n"
-                 "   0, 1, 3, 4, 6, 7, 8, 9, 10, 100, 101, 103 -> not available in this engine\n\n"
-                 "Options:\n"
-                 "   --bs <block size>         block size for RTX_blocks (default: 2^15)\n"
-                 "   --nb <#blocks>            number of blocks for RTX_blocks (overrides --bs)\n"
-                 "   --reps <repetitions>      RMQ repeats for the avg time (default: 10)\n"
-                 "   --dev <device ID>         device ID (default: 0)\n"
-                 "   --nt  <thread num>        number of CPU threads (query generation)\n"
-                 "   --seed <seed>             seed for PRNG\n"
-                 "   --check                   check correctness against GPU BASE\n"
-                 "   --save-time=<file>        append a CSV row\n"
-                 "   --save-power=<file>       sample GPU power (NVML) around the timed loop\n",
-                 kAlgStr[2], kAlgStr[5]);
+                 "usage: rtxrmq <n> <q> <lr> <alg> [options]\n"
+                 "\n"
+                 "Builds a range-minimum index over n random float32 values and answers q\n"
+                 "random inclusive queries (l, r) on the GPU, timing the query launches.\n"
+                 "\n"
+                 "positional arguments\n"
+                 "  n     array length (1 .. 2^31-1)\n"
+                 "  q     number of queries\n"
+                 "  lr    query length: a positive value fixes every length (at most n);\n"
+                 "        -1 draws lengths uniformly from [1, n], -2 / -3 from lognormal\n"
+                 "        distributions centred near n^0.6 / n^0.3, -4 / -5 near n/2^8 and\n"
+                 "        n/2^15\n"
+                 "  alg   5 = block decomposition (%s), returning minimum values\n"
+                 "        2 = brute force on the GPU (%s), returning minimum values\n"
+                 "        105, 102 = the same two, returning leftmost argmin indices\n"
+                 "        (every other id of the original tool exits with status 2 here)\n"
+                 "\n"
+                 "options\n"
+                 "  --bs <k>            elements per block for alg 5 (default 32768)\n"
+                 "  --nb <k>            number of blocks instead; block size = n / k\n"
+                 "  --reps <k>          timed repetitions of the query launch (default 10)\n"
+                 "  --dev <id>          CUDA device (default 0)\n"
+                 "  --nt <k>            host threads for generating the queries\n"
+                 "  --seed <s>          generator seed (default: the current time)\n"
+                 "  --check             compare every answer with the brute force\n"
+                 "  --save-time=<file>  append one CSV row of timings\n"
+                 "  --save-power=<file> record board power (NVML) over the timed loop\n",
+                 kAlgStr[5], kAlgStr[2]);
 }
 
 const char *alg_name(int alg) { return kAlgStr[alg % 100 <= 10 ? alg % 100 : 0]; }
