@@ -201,15 +201,19 @@ def test_finite_differences_thousands(cuda, native):
     g64 = gout.astype(np.float64)
     xd = torch.from_numpy(x).to(cuda)
 
-    def loss(j, delta):
+    def loss(j, xj):
         with torch.no_grad():
-            xd[j] = float(x[j]) + delta
+            xd[j] = float(xj)
             yv, _ = m(xd, dQ)
             xd[j] = float(x[j])
         return float((yv.cpu().numpy().astype(np.float64) * g64).sum())
 
+    # divided by the float32 values actually stored, x[j] +- eps rounded
     eps = 1e-3
-    fd = np.array([(loss(j, eps) - loss(j, -eps)) / (2 * eps) for j in range(n)])
+    fd = np.empty(n)
+    for j in range(n):
+        xp, xm = np.float32(x[j] + eps), np.float32(x[j] - eps)
+        fd[j] = (loss(j, xp) - loss(j, xm)) / (float(xp) - float(xm))
     nz = np.abs(grad) > 0
     assert nz.sum() > 100
     assert np.all(np.abs(fd[~nz]) < 1e-6)
