@@ -324,6 +324,33 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts,
                      const int64_t *h_qcounts, const int32_t *h_bucket_bs,
                      rmq_batch_t **out);
 
+/*
+ * Block size and tile schedule of one size bucket: the plan cuts each array
+ * of the bucket into query items of query_chunk queries (the unit of work a
+ * CTA takes in the query phase) and each sparse-table level into items of
+ * level_chunk entries (the unit of the table phase). Values <= 0 mean the
+ * defaults (bs as rmq_batch_create, 2048 queries, 4096 entries). The
+ * reference has no batched form, so no counterpart.
+ */
+typedef struct rmq_batch_tile {
+    int32_t bs;
+    int32_t query_chunk;
+    int32_t level_chunk;
+    int32_t reserved;
+} rmq_batch_tile_t;
+
+/* rmq_batch_create with a tile per bucket (h_bucket_tiles: RMQ_BATCH_BUCKETS
+ * entries, or NULL for the defaults). rmq_batch_create(..., bs, out) is this
+ * call with tiles {bs[b], 0, 0, 0}. */
+int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts,
+                        const int64_t *h_lengths, const int64_t *h_qstarts,
+                        const int64_t *h_qcounts,
+                        const rmq_batch_tile_t *h_bucket_tiles,
+                        rmq_batch_t **out);
+
+/* The plan's tile per bucket (RMQ_BATCH_BUCKETS entries, defaults filled in). */
+int rmq_batch_tiles(const rmq_batch_t *b, rmq_batch_tile_t *h_bucket_tiles);
+
 /* Build every array and answer every query: one cooperative launch. */
 int rmq_batch_run(rmq_batch_t *b, const float *d_vals,
                   const int32_t *d_queries, float *d_val, int32_t *d_idx,
@@ -379,6 +406,21 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts,
                        const int32_t *d_queries, float *d_val, int32_t *d_idx,
                        int32_t reps, rmq_stream_t stream,
                        int32_t *h_bucket_bs);
+
+/*
+ * rmq_batch_autotune over the whole tile: per bucket present, first the
+ * block size (as rmq_batch_autotune), then with it the query-item size
+ * (512 .. 8192 queries) and then the level-item size (1024 .. 16384
+ * entries), each the fastest over `reps` runs of a plan holding only that
+ * bucket's arrays; absent buckets get {0, 0, 0, 0}. Allocates and frees
+ * temporary plans; d_val / d_idx are scratch outputs.
+ */
+int rmq_batch_autotune_ex(int32_t narrays, const int64_t *h_starts,
+                          const int64_t *h_lengths, const int64_t *h_qstarts,
+                          const int64_t *h_qcounts, const float *d_vals,
+                          const int32_t *d_queries, float *d_val,
+                          int32_t *d_idx, int32_t reps, rmq_stream_t stream,
+                          rmq_batch_tile_t *h_bucket_tiles);
 
 /*
  * GPU power sampling around a timed region, the role of the reference's

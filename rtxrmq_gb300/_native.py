@@ -50,6 +50,11 @@ class rmq_batch_info_t(C.Structure):
                 ("query_items", C.c_int32), ("bucket_bs", C.c_int32 * RMQ_BATCH_BUCKETS)]
 
 
+class rmq_batch_tile_t(C.Structure):
+    _fields_ = [("bs", C.c_int32), ("query_chunk", C.c_int32), ("level_chunk", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 _vp, _i64, _i32, _u64, _dbl = C.c_void_p, C.c_int64, C.c_int32, C.c_uint64, C.c_double
 
 # name -> (restype, argtypes); every symbol include/rmq.h declares
@@ -73,6 +78,9 @@ SIGNATURES = {
     "rmq_probe_random": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_checked_violations": (C.c_int, [C.POINTER(_i64)]),
     "rmq_batch_create": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "rmq_batch_create_ex": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "rmq_batch_tiles": (C.c_int, [_vp, _vp]),
+    "rmq_batch_autotune_ex": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp]),
     "rmq_batch_run": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_run_per_array": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_build": (C.c_int, [_vp, _vp, _vp]),

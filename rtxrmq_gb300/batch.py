@@ -5,8 +5,10 @@ Thousands of independent float32 arrays of uneven length, each with its own
 launch. ``run_per_array`` produces the same results through the plain path
 (one build + one query launch sequence per array) for comparison.
 ``autotune`` picks the block size of every size bucket (floor(log2 length))
-by timing the candidates on the actual arrays and queries, and caches the
-choice per GPU model, bucket and query-length class.
+by timing the candidates on the actual arrays and queries, and with
+``tiles=True`` also the bucket's tile schedule (queries per query item,
+table entries per level item); it caches the choice per GPU model, bucket
+and query-length class.
 """
 from __future__ import annotations
 
@@ -18,7 +20,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from ._native import RMQ_BATCH_BUCKETS, check, load, rmq_batch_info_t
+from ._native import RMQ_BATCH_BUCKETS, check, load, rmq_batch_info_t, rmq_batch_tile_t
 
 __all__ = ["RMQBatch", "autotune", "bucket_of", "DEFAULT_CACHE"]
 
@@ -66,28 +68,36 @@ def _queries(t):
     return _dptr(t)
 
 
+def _tile_array(tiles):
+    """RMQ_BATCH_BUCKETS rmq_batch_tile_t from per-bucket block sizes (ints)
+    or (bs, query_chunk, level_chunk) triples; missing buckets are 0."""
+    arr = (rmq_batch_tile_t * RMQ_BATCH_BUCKETS)()
+    for b, t in enumerate(list(tiles)[:RMQ_BATCH_BUCKETS]):
+        t = (int(t), 0, 0) if np.isscalar(t) else tuple(int(x) for x in t)
+        arr[b].bs, arr[b].query_chunk, arr[b].level_chunk = t
+    return arr
+
+
 class RMQBatch:
     """A planned batch: array i is values[starts[i] : starts[i] + lengths[i]]
     and owns queries[qstarts[i] : qstarts[i] + qcounts[i]] (array-local
-    int32 (l, r) pairs). ``bucket_bs`` maps size bucket -> block size."""
+    int32 (l, r) pairs). ``bucket_bs`` maps size bucket -> block size, or
+    -> (block size, queries per query item, entries per level item) as
+    ``autotune(..., tiles=True)`` returns."""
 
     def __init__(self, starts: Sequence[int], lengths: Sequence[int], qstarts: Sequence[int],
-                 qcounts: Sequence[int], bucket_bs: Optional[Sequence[int]] = None):
+                 qcounts: Sequence[int], bucket_bs: Optional[Sequence] = None):
         self.starts, self.lengths = _i64(starts), _i64(lengths)
         self.qstarts, self.qcounts = _i64(qstarts), _i64(qcounts)
         n = len(self.starts)
         if not (len(self.lengths) == len(self.qstarts) == len(self.qcounts) == n):
             raise ValueError("starts, lengths, qstarts, qcounts must have the same length")
-        cfg = None
-        if bucket_bs is not None:
-            cfg = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
-            b = np.asarray(bucket_bs, dtype=np.int32)[:RMQ_BATCH_BUCKETS]
-            cfg[:len(b)] = b
-        self._cfg = cfg
+        tiles = None if bucket_bs is None else _tile_array(bucket_bs)
         self._h = C.c_void_p()
-        check(load().rmq_batch_create(n, self.starts.ctypes.data, self.lengths.ctypes.data,
-                                      self.qstarts.ctypes.data, self.qcounts.ctypes.data,
-                                      None if cfg is None else cfg.ctypes.data, C.byref(self._h)))
+        check(load().rmq_batch_create_ex(n, self.starts.ctypes.data, self.lengths.ctypes.data,
+                                         self.qstarts.ctypes.data, self.qcounts.ctypes.data,
+                                         None if tiles is None else C.addressof(tiles),
+                                         C.byref(self._h)))
 
     def _out(self, queries, out_val, out_idx, values: bool, indices: bool):
         import torch
@@ -141,6 +151,13 @@ class RMQBatch:
         d["bucket_bs"] = list(inf.bucket_bs)
         return d
 
+    def tiles(self) -> list:
+        """(block size, queries per query item, entries per level item) per
+        size bucket, defaults filled in (block size 0: the default rule)."""
+        arr = (rmq_batch_tile_t * RMQ_BATCH_BUCKETS)()
+        check(load().rmq_batch_tiles(self._h, C.addressof(arr)))
+        return [(t.bs, t.query_chunk, t.level_chunk) for t in arr]
+
     def invalid_count(self, stream=None) -> int:
         v = C.c_int64()
         check(load().rmq_batch_invalid_count(self._h, _stream(stream), C.byref(v)))
@@ -187,40 +204,50 @@ def _cache_keys(lengths, qstarts, qcounts, queries_host) -> dict:
 
 def autotune(starts, lengths, qstarts, qcounts, vals, queries, *, reps: int = 3,
              queries_host: Optional[np.ndarray] = None, cache: Optional[Path] = DEFAULT_CACHE,
-             stream=None) -> list:
-    """Per-bucket block sizes for this batch (RMQ_BATCH_BUCKETS entries).
+             stream=None, tiles: bool = False) -> list:
+    """Per-bucket block sizes for this batch (RMQ_BATCH_BUCKETS entries), or
+    with ``tiles=True`` per-bucket (block size, queries per query item,
+    entries per level item) triples (rmq_batch_autotune_ex).
 
     Cached results (per GPU model and bucket/query-length key) are reused;
-    missing buckets are timed by rmq_batch_autotune on the real data."""
+    missing buckets are timed on the real data."""
     import torch
     starts, lengths = _i64(starts), _i64(lengths)
     qstarts, qcounts = _i64(qstarts), _i64(qcounts)
     dev = torch.cuda.get_device_name()
-    keys = _cache_keys(lengths, qstarts, qcounts, queries_host)
+    keys = {b: k + ("_tiles" if tiles else "")
+            for b, k in _cache_keys(lengths, qstarts, qcounts, queries_host).items()}
     table = {}
     if cache is not None and Path(cache).exists():
         try:
             table = json.loads(Path(cache).read_text()).get(dev, {})
         except (OSError, ValueError):
             table = {}
-    out = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
+    empty = (0, 0, 0) if tiles else 0
+    out = [empty] * RMQ_BATCH_BUCKETS
     missing = [b for b, k in keys.items() if k not in table]
     for b, k in keys.items():
         if k in table:
-            out[b] = int(table[k])
+            out[b] = tuple(table[k]) if tiles else int(table[k])
     if missing:
         sel = np.nonzero(np.isin(bucket_of(lengths), missing))[0]
-        res = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
         qn = int(queries.shape[0])
         sv = torch.empty(qn, dtype=torch.float32, device=queries.device)
         si = torch.empty(qn, dtype=torch.int32, device=queries.device)
         s_, l_, qs_, qc_ = (np.ascontiguousarray(x[sel]) for x in (starts, lengths, qstarts, qcounts))
-        check(load().rmq_batch_autotune(len(sel), s_.ctypes.data, l_.ctypes.data, qs_.ctypes.data,
-                                        qc_.ctypes.data, _dptr(vals), _dptr(queries), _dptr(sv),
-                                        _dptr(si), int(reps), _stream(stream), res.ctypes.data))
+        args = (len(sel), s_.ctypes.data, l_.ctypes.data, qs_.ctypes.data, qc_.ctypes.data,
+                _dptr(vals), _dptr(queries), _dptr(sv), _dptr(si), int(reps), _stream(stream))
+        if tiles:
+            res = (rmq_batch_tile_t * RMQ_BATCH_BUCKETS)()
+            check(load().rmq_batch_autotune_ex(*args, C.addressof(res)))
+            got = [(t.bs, t.query_chunk, t.level_chunk) for t in res]
+        else:
+            res = np.zeros(RMQ_BATCH_BUCKETS, dtype=np.int32)
+            check(load().rmq_batch_autotune(*args, res.ctypes.data))
+            got = [int(x) for x in res]
         for b in missing:
-            out[b] = res[b]
-            table[keys[b]] = int(res[b])
+            out[b] = got[b]
+            table[keys[b]] = list(got[b]) if tiles else got[b]
         if cache is not None:
             try:
                 Path(cache).parent.mkdir(parents=True, exist_ok=True)
@@ -229,4 +256,4 @@ def autotune(starts, lengths, qstarts, qcounts, vals, queries, *, reps: int = 3,
                 Path(cache).write_text(json.dumps(full, indent=1, sort_keys=True))
             except (OSError, ValueError):
                 pass
-    return [int(x) for x in out]
+    return out

@@ -40,8 +40,10 @@ namespace {
 
 constexpr int kThreads = kBuildThreads;  // phase A runs the unit builder
 constexpr int kQPT = 2;
-constexpr uint32_t kQueryChunk = 2048;  // queries per query item
-constexpr uint32_t kLevelChunk = 4096;  // sparse-table entries per level item
+// default tile schedule: queries per query item, sparse-table entries per
+// level item (a plan can set both per size bucket, rmq_batch_create_ex)
+constexpr uint32_t kQueryChunk = 2048;
+constexpr uint32_t kLevelChunk = 4096;
 constexpr int kMaxLevels = 32;
 
 struct BatchArray {
@@ -201,6 +203,7 @@ struct rmq_batch {
     size_t ws_bytes;
     BatchParams P;       // device pointers filled, per-run fields left empty
     int32_t bucket_bs[RMQ_BATCH_BUCKETS];
+    rmq_batch_tile_t tiles[RMQ_BATCH_BUCKETS];  // block size and tile schedule per bucket
     const float *built_vals;  // values of the last build enqueued on this plan
 };
 
@@ -218,16 +221,147 @@ int64_t default_bs(int64_t n) {
 
 }  // namespace
 
+namespace {
+
+// Milliseconds of `reps` runs (after one warm run) of a plan holding only
+// the arrays `m`, with tile `t` for their bucket bk; <0 on failure (rc set).
+float time_bucket(const std::vector<int64_t> &s, const std::vector<int64_t> &l,
+                  const std::vector<int64_t> &qs, const std::vector<int64_t> &qc, int bk,
+                  const rmq_batch_tile_t &t, const float *d_vals, const int32_t *d_queries,
+                  float *d_val, int32_t *d_idx, int32_t reps, rmq_stream_t stream,
+                  cudaEvent_t e0, cudaEvent_t e1, int &rc) {
+    rmq_batch_tile_t cfg[RMQ_BATCH_BUCKETS];
+    std::memset(cfg, 0, sizeof(cfg));
+    cfg[bk] = t;
+    rmq_batch_t *sub = nullptr;
+    rc = rmq_batch_create_ex(static_cast<int32_t>(s.size()), s.data(), l.data(), qs.data(),
+                             qc.data(), cfg, &sub);
+    if (rc) return -1.f;
+    rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);  // warm
+    float ms = -1.f;
+    if (!rc) {
+        cudaEventRecord(e0, stream);
+        for (int r = 0; r < reps && !rc; ++r)
+            rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);
+        cudaEventRecord(e1, stream);
+        const cudaError_t err = cudaEventSynchronize(e1);
+        if (err != cudaSuccess && !rc) rc = cuda_fail(err, "rmq_batch_autotune: timing");
+        if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+    }
+    rmq_batch_free(sub);
+    return rc ? -1.f : ms;
+}
+
+// Per size bucket: the block size, then (tiles == true) the query-item and
+// level-item sizes, each the fastest candidate on that bucket's arrays and
+// queries with the choices made so far.
+int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
+                     const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
+                     const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
+                     rmq_stream_t stream, rmq_batch_tile_t *out, bool tiles) {
+    NvtxRange nvtx_range("rmq_batch_autotune");
+    if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts)
+        return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
+    if (reps < 1) reps = 1;
+    std::vector<std::vector<int32_t>> members(RMQ_BATCH_BUCKETS);
+    for (int32_t i = 0; i < narrays; ++i) {
+        if (h_lengths[i] < 0) return set_error(RMQ_EINVAL, "rmq_batch_autotune: array %d length < 0", i);
+        if (h_lengths[i] > 0) members[bucket_of(h_lengths[i])].push_back(i);  // empty: no structure
+    }
+    static const int32_t bs_cands[] = {64, 256, 1024, 4096, 16384, 65536};
+    static const int32_t q_cands[] = {512, 1024, 2048, 4096, 8192};
+    static const int32_t l_cands[] = {1024, 4096, 16384};
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_autotune: events");
+    int rc = RMQ_OK;
+    for (int bk = 0; bk < RMQ_BATCH_BUCKETS; ++bk) out[bk] = rmq_batch_tile_t{0, 0, 0, 0};
+    for (int bk = 0; bk < RMQ_BATCH_BUCKETS && rc == RMQ_OK; ++bk) {
+        const std::vector<int32_t> &m = members[bk];
+        if (m.empty()) continue;
+        std::vector<int64_t> s, l, qs, qc;
+        for (int32_t i : m) {
+            s.push_back(h_starts[i]);
+            l.push_back(h_lengths[i]);
+            qs.push_back(h_qstarts[i]);
+            qc.push_back(h_qcounts[i]);
+        }
+        const int64_t maxlen = int64_t(2) << bk;
+        rmq_batch_tile_t best{0, static_cast<int32_t>(kQueryChunk), static_cast<int32_t>(kLevelChunk), 0};
+        float best_ms = 0.f;
+        for (int32_t c : bs_cands) {
+            if (c > 2 * maxlen && best.bs != 0) break;
+            rmq_batch_tile_t t = best;
+            t.bs = c;
+            const float ms = time_bucket(s, l, qs, qc, bk, t, d_vals, d_queries, d_val, d_idx,
+                                         reps, stream, e0, e1, rc);
+            if (rc) break;
+            if (best.bs == 0 || ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
+        for (int32_t c : q_cands) {
+            if (!tiles || rc) break;
+            if (c == best.query_chunk) continue;
+            rmq_batch_tile_t t = best;
+            t.query_chunk = c;
+            const float ms = time_bucket(s, l, qs, qc, bk, t, d_vals, d_queries, d_val, d_idx,
+                                         reps, stream, e0, e1, rc);
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
+        for (int32_t c : l_cands) {
+            if (!tiles || rc) break;
+            if (c == best.level_chunk) continue;
+            rmq_batch_tile_t t = best;
+            t.level_chunk = c;
+            const float ms = time_bucket(s, l, qs, qc, bk, t, d_vals, d_queries, d_val, d_idx,
+                                         reps, stream, e0, e1, rc);
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
+        out[bk] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+}  // namespace
+
 extern "C" {
 
 int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
                      const int64_t *h_qstarts, const int64_t *h_qcounts,
                      const int32_t *h_bucket_bs, rmq_batch_t **out) {
+    rmq_batch_tile_t tiles[RMQ_BATCH_BUCKETS];
+    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) {
+        tiles[i].bs = h_bucket_bs ? h_bucket_bs[i] : 0;
+        tiles[i].query_chunk = 0;
+        tiles[i].level_chunk = 0;
+        tiles[i].reserved = 0;
+    }
+    return rmq_batch_create_ex(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, tiles, out);
+}
+
+int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
+                        const int64_t *h_qstarts, const int64_t *h_qcounts,
+                        const rmq_batch_tile_t *h_bucket_tiles, rmq_batch_t **out) {
     NvtxRange nvtx_range("rmq_batch_create");
     if (!out) return set_error(RMQ_EINVAL, "rmq_batch_create: out is NULL");
     *out = nullptr;
     if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts)
         return set_error(RMQ_EINVAL, "rmq_batch_create: narrays must be > 0 and arrays non-NULL");
+    if (h_bucket_tiles)
+        for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i)
+            if (h_bucket_tiles[i].query_chunk < 0 || h_bucket_tiles[i].level_chunk < 0)
+                return set_error(RMQ_EINVAL, "rmq_batch_create: bucket %d has a negative chunk", i);
     DeviceInfo dev;
     int rc = device_info(&dev);
     if (rc) return rc;
@@ -240,8 +374,14 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
     b->limit = 0;
     b->total_q = 0;
     b->mem = nullptr;
-    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i)
-        b->bucket_bs[i] = h_bucket_bs && h_bucket_bs[i] > 0 ? h_bucket_bs[i] : 0;
+    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) {
+        const rmq_batch_tile_t t = h_bucket_tiles ? h_bucket_tiles[i] : rmq_batch_tile_t{0, 0, 0, 0};
+        b->bucket_bs[i] = t.bs > 0 ? t.bs : 0;
+        b->tiles[i].bs = b->bucket_bs[i];
+        b->tiles[i].query_chunk = t.query_chunk > 0 ? t.query_chunk : static_cast<int32_t>(kQueryChunk);
+        b->tiles[i].level_chunk = t.level_chunk > 0 ? t.level_chunk : static_cast<int32_t>(kLevelChunk);
+        b->tiles[i].reserved = 0;
+    }
 
     std::vector<uint2> build;
     std::vector<std::vector<uint4>> lvl(kMaxLevels);
@@ -259,8 +399,11 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
                              i, (long long)s, (long long)n, (long long)qs, (long long)qc);
         }
         // an empty array has no structure; its queries (if any) are invalid
-        int64_t bs = n > 0 ? b->bucket_bs[bucket_of(n)] : 1;
+        const int bk = n > 0 ? bucket_of(n) : 0;
+        int64_t bs = n > 0 ? b->bucket_bs[bk] : 1;
         if (bs <= 0) bs = default_bs(n);
+        const uint32_t qchunk = static_cast<uint32_t>(b->tiles[bk].query_chunk);
+        const uint32_t lchunk = static_cast<uint32_t>(b->tiles[bk].level_chunk);
         if (bs > n) bs = n > 0 ? n : 1;
         BatchArray &a = b->h_arrays[i];
         a.off = s;
@@ -283,12 +426,12 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
         for (uint32_t u = 0; u < nunits; ++u) build.push_back(make_uint2(i, u));
         for (uint32_t k = 1; k < a.levels; ++k) {
             const uint32_t cnt = a.nb - (1u << k) + 1;
-            for (uint32_t j = 0; j < cnt; j += kLevelChunk)
-                lvl[k].push_back(make_uint4(i, k, j, std::min(kLevelChunk, cnt - j)));
+            for (uint32_t j = 0; j < cnt; j += lchunk)
+                lvl[k].push_back(make_uint4(i, k, j, std::min(lchunk, cnt - j)));
         }
-        for (int64_t j = 0; j < qc; j += kQueryChunk)
+        for (int64_t j = 0; j < qc; j += qchunk)
             b->h_qitems.push_back(make_uint4(i, static_cast<uint32_t>(j),
-                                             static_cast<uint32_t>(std::min<int64_t>(kQueryChunk, qc - j)), 0));
+                                             static_cast<uint32_t>(std::min<int64_t>(qchunk, qc - j)), 0));
     }
     if (b->limit > 0xffffffffLL * 4) {
         delete b;
@@ -512,6 +655,12 @@ int rmq_batch_info(const rmq_batch_t *b, rmq_batch_info_t *info) {
     return RMQ_OK;
 }
 
+int rmq_batch_tiles(const rmq_batch_t *b, rmq_batch_tile_t *h_bucket_tiles) {
+    if (!b || !h_bucket_tiles) return set_error(RMQ_EINVAL, "rmq_batch_tiles: NULL argument");
+    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) h_bucket_tiles[i] = b->tiles[i];
+    return RMQ_OK;
+}
+
 int rmq_batch_invalid_count(const rmq_batch_t *b, rmq_stream_t stream, int64_t *count) {
     if (!b || !count) return set_error(RMQ_EINVAL, "rmq_batch_invalid_count: NULL argument");
     unsigned long long v = 0;
@@ -534,64 +683,21 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts, const int64_t *
                        const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
                        const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
                        rmq_stream_t stream, int32_t *h_bucket_bs) {
-    NvtxRange nvtx_range("rmq_batch_autotune");
-    if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts || !h_bucket_bs)
-        return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
-    if (reps < 1) reps = 1;
-    std::vector<std::vector<int32_t>> members(RMQ_BATCH_BUCKETS);
-    for (int32_t i = 0; i < narrays; ++i) {
-        if (h_lengths[i] < 0) return set_error(RMQ_EINVAL, "rmq_batch_autotune: array %d length < 0", i);
-        if (h_lengths[i] > 0) members[bucket_of(h_lengths[i])].push_back(i);  // empty: no structure
-    }
-    static const int32_t cands[] = {64, 256, 1024, 4096, 16384, 65536};
-    cudaEvent_t e0, e1;
-    cudaError_t err = cudaEventCreate(&e0);
-    if (err == cudaSuccess) err = cudaEventCreate(&e1);
-    if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_autotune: events");
-    int rc = RMQ_OK;
-    for (int bk = 0; bk < RMQ_BATCH_BUCKETS && rc == RMQ_OK; ++bk) {
-        h_bucket_bs[bk] = 0;
-        const std::vector<int32_t> &m = members[bk];
-        if (m.empty()) continue;
-        std::vector<int64_t> s, l, qs, qc;
-        for (int32_t i : m) {
-            s.push_back(h_starts[i]);
-            l.push_back(h_lengths[i]);
-            qs.push_back(h_qstarts[i]);
-            qc.push_back(h_qcounts[i]);
-        }
-        const int64_t maxlen = int64_t(2) << bk;
-        float best_ms = 0.f;
-        for (int32_t c : cands) {
-            if (c > 2 * maxlen && h_bucket_bs[bk] != 0) break;
-            int32_t cfg[RMQ_BATCH_BUCKETS] = {0};
-            cfg[bk] = c;
-            rmq_batch_t *sub = nullptr;
-            rc = rmq_batch_create(static_cast<int32_t>(m.size()), s.data(), l.data(), qs.data(),
-                                  qc.data(), cfg, &sub);
-            if (rc) break;
-            rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);  // warm
-            if (!rc) {
-                cudaEventRecord(e0, stream);
-                for (int r = 0; r < reps && !rc; ++r)
-                    rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);
-                cudaEventRecord(e1, stream);
-                err = cudaEventSynchronize(e1);
-                if (err != cudaSuccess && !rc) rc = cuda_fail(err, "rmq_batch_autotune: timing");
-            }
-            float ms = 0.f;
-            if (!rc) cudaEventElapsedTime(&ms, e0, e1);
-            rmq_batch_free(sub);
-            if (rc) break;
-            if (h_bucket_bs[bk] == 0 || ms < best_ms) {
-                best_ms = ms;
-                h_bucket_bs[bk] = c;
-            }
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (!h_bucket_bs) return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
+    rmq_batch_tile_t tiles[RMQ_BATCH_BUCKETS];
+    const int rc = autotune_buckets(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, d_vals,
+                                    d_queries, d_val, d_idx, reps, stream, tiles, false);
+    for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) h_bucket_bs[i] = rc ? 0 : tiles[i].bs;
     return rc;
+}
+
+int rmq_batch_autotune_ex(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
+                          const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
+                          const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
+                          rmq_stream_t stream, rmq_batch_tile_t *h_bucket_tiles) {
+    if (!h_bucket_tiles) return set_error(RMQ_EINVAL, "rmq_batch_autotune_ex: NULL argument");
+    return autotune_buckets(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, d_vals, d_queries,
+                            d_val, d_idx, reps, stream, h_bucket_tiles, true);
 }
 
 }  // extern "C"

@@ -305,3 +305,43 @@ def test_batch_build_once_query_many(cuda, native, oracle_lib):
         torch.cuda.synchronize()
         G = Q.astype(np.int64) + off[:, None]
         np.testing.assert_array_equal(i.cpu().numpy() + off, oracle.base_idx(V, G))
+
+
+def test_autotune_tiles(cuda, native, oracle_lib, tmp_path):
+    """The tile autotuner picks per bucket a block size, a query-item size
+    and a level-item size from its candidates; the plan reports them, the
+    cache returns them, and the answers do not depend on them."""
+    import torch
+
+    from rtxrmq_gb300.batch import RMQBatch, autotune, bucket_of
+    starts, lengths, qstarts, qcounts, A, Q = small_ragged(5, False, 4)
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    cache = tmp_path / "tiles.json"
+    cfg = autotune(starts, lengths, qstarts, qcounts, dA, dQ, reps=1, queries_host=Q, cache=cache,
+                   tiles=True)
+    present = set(int(b) for b in bucket_of(lengths))
+    for bk in range(32):
+        if bk in present:
+            assert cfg[bk][0] in (64, 256, 1024, 4096, 16384, 65536)
+            assert cfg[bk][1] in (512, 1024, 2048, 4096, 8192)
+            assert cfg[bk][2] in (1024, 4096, 16384)
+        else:
+            assert cfg[bk] == (0, 0, 0)
+    assert autotune(starts, lengths, qstarts, qcounts, dA, dQ, queries_host=Q, cache=cache,
+                    tiles=True) == cfg
+    ev, ei = expected(oracle_lib, starts, lengths, qstarts, qcounts, A, Q)
+    own = owned_mask(qstarts, qcounts, len(Q))
+    with RMQBatch(starts, lengths, qstarts, qcounts, cfg) as b:
+        got = b.tiles()
+        for bk in present:
+            assert got[bk] == cfg[bk]
+        v, i = b.run(dA, dQ)
+        np.testing.assert_array_equal(i.cpu().numpy()[own], ei[own])
+    # extreme schedules give the same answers
+    for qc, lc in ((1, 1), (7, 3), (1 << 20, 1 << 20)):
+        with RMQBatch(starts, lengths, qstarts, qcounts, [(256, qc, lc)] * 32) as b:
+            v, i = b.run(dA, dQ)
+            np.testing.assert_array_equal(i.cpu().numpy()[own], ei[own])
+            np.testing.assert_array_equal(v.cpu().numpy()[own].view(np.uint32),
+                                          ev[own].view(np.uint32))
