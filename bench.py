@@ -602,16 +602,18 @@ def bench_batched(args, dev, stream, barrier):
     oi = torch.empty(w.total_q, dtype=torch.int32, device=dev)
     t = time.perf_counter()
     if args.batch_bs:
-        cfg = [args.batch_bs] * 32
+        cfg = [(args.batch_bs, 0, 0)] * 32
     else:
+        # per bucket: block size, queries per query item, entries per level item
         cfg = autotune(w.starts, w.lengths, w.qstarts, w.qcounts, dV, dQ, reps=2,
-                       queries_host=w.queries, cache=None)
+                       queries_host=w.queries, cache=None, tiles=True)
     tune_s = time.perf_counter() - t
     res = {"workload": "4096 arrays, len round(2^U) U~U[8,22], 2^26 queries proportional to "
                        "length, query len lognormal(0.5 ln len, 0.4), values U[0,1)",
            "arrays": int(len(w.lengths)), "elements": int(w.lengths.sum()), "queries": w.total_q,
            "generate_s": gen_s, "autotune_s": tune_s,
-           "bucket_bs": {str(b): v for b, v in enumerate(cfg) if v}}
+           "bucket_tiles": {str(b): {"bs": v[0], "query_chunk": v[1], "level_chunk": v[2]}
+                            for b, v in enumerate(cfg) if v[0]}}
     with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, cfg) as b:
         info = b.info()
         res["workspace_gb"] = info["workspace_bytes"] / 1e9
@@ -667,7 +669,7 @@ def bench_autograd(args, dev, stream, barrier):
     gout_h = np.random.default_rng(SEED).standard_normal(d.total_q).astype(np.float32)
     go = torch.from_numpy(gout_h).to(dev)
     cfg = autotune(d.starts, d.lengths, d.qstarts, d.qcounts, x, dQ, reps=2,
-                   queries_host=d.queries, cache=None)
+                   queries_host=d.queries, cache=None, tiles=True)
     m = RaggedRangeMin(d.lengths, d.qcounts, cfg)
     xg = x.clone().requires_grad_(True)
 
@@ -704,7 +706,9 @@ def bench_autograd(args, dev, stream, barrier):
     q = d.total_q
     res = {"workload": "256 rows N(0,1), len U[2^14,2^20], 2^16 ranges/row, len lognormal("
                        "0.4 ln len, 0.5), grad_out N(0,1)",
-           "elements": d.span, "queries": q, "bucket_bs": {str(b): v for b, v in enumerate(cfg) if v},
+           "elements": d.span, "queries": q,
+           "bucket_tiles": {str(b): {"bs": v[0], "query_chunk": v[1], "level_chunk": v[2]}
+                            for b, v in enumerate(cfg) if v[0]},
            "fwd_ms": fms, "fwd_bwd_ms": bms, "fwd_bwd_over_fwd": bms / fms,
            "fwd_rmq_s": job_rate(q, world()[1], fms), "fwd_bwd_rmq_s": job_rate(q, world()[1], bms),
            "graph_captured": True, "grad_max_rel_err_vs_fp64": rel, "grad_zero_elsewhere": zero_ok}
