@@ -147,7 +147,11 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
         grid.sync();
     }
 
-    // C: queries
+    // C: queries, in the queued form; the warps' miss queues live in the
+    // staging memory of phase A
+    static_assert(sizeof(MissQueue) * (kThreads / 32) <= sizeof(Entry) * kStageEntries,
+                  "miss queues fit the staging memory");
+    MissQueue &mq = reinterpret_cast<MissQueue *>(stage)[threadIdx.x >> 5];
     for (int32_t it = (P.phases & 4u) ? blockIdx.x : P.nqitems; it < P.nqitems; it += gridDim.x) {
         const uint4 w = P.qitems[it];
         const BatchArray a = P.arrays[w.x];
@@ -158,7 +162,8 @@ __global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchPa
         o.idx = P.idx ? P.idx + a.qoff : nullptr;
         o.invalid = P.invalid;
         o.span = P.total_q - a.qoff;
-        answer_range<ALIGNED, kQPT>(v, o, w.y, static_cast<int64_t>(w.y) + w.z);
+        answer_range_queued<ALIGNED, false, kFloatMin, kThreads, kQPT>(
+            v, o, w.y, static_cast<int64_t>(w.y) + w.z, mq);
     }
 }
 

@@ -118,6 +118,18 @@ __device__ __forceinline__ uint32_t ld_moff(const V1View &v, uint64_t i, uint64_
     return r;
 }
 
+// The aligned 8-byte word of the 1-byte micro-table offsets that holds
+// offset i (the table starts 256-byte aligned; its tail is padded to 256
+// bytes, so the word never passes the allocation).
+__device__ __forceinline__ uint64_t ld_moff_word(const V1View &v, uint64_t i, uint64_t pol) {
+    const uint64_t w = i >> 3;
+    if (!rmq_chk(w < (static_cast<uint64_t>(v.mlevels - 1u) * v.nmicro + 7) / 8)) return 0u;
+    uint64_t r;
+    asm volatile("ld.global.L2::cache_hint.u64 %0, [%1], %2;"
+                 : "=l"(r) : "l"(static_cast<const uint64_t *>(v.moff) + w), "l"(pol));
+    return r;
+}
+
 // Leftmost minimum of local A[a..b] (b - a < 32) computed by one thread.
 // ALIGNED: 16-byte loads of the chunks covering [a, b] (at most 9), two per
 // round, so that few registers are live.
@@ -609,17 +621,29 @@ __device__ __forceinline__ Entry superset_probe(const V1View &v, uint32_t l, uin
     const int lev = ilog2(b - a + 1u);
     uint32_t x = a, y = b + 1u - (1u << lev);
     if (MICRO && mic) {
-        // lev >= 1: the query spans at least two micro-blocks
+        // lev >= 1: the query spans at least two micro-blocks. The two
+        // windows overlap, so 1-byte offsets often share an aligned 8-byte
+        // word (one load), and both windows often point at the same best
+        // micro-block (one minimum load).
         const uint64_t row = static_cast<uint64_t>(lev - 1) * v.nmicro;
-        x += ld_moff(v, row + x, pol);
-        y += ld_moff(v, row + y, pol);
-        if constexpr (STATS) s.c[kStatTable] += 2u;
+        if (v.moff_bytes == 1u && ((row + x) >> 3) == ((row + y) >> 3)) {
+            const uint64_t w = ld_moff_word(v, row + x, pol);
+            x += static_cast<uint32_t>(w >> (8 * ((row + x) & 7))) & 0xffu;
+            y += static_cast<uint32_t>(w >> (8 * ((row + y) & 7))) & 0xffu;
+            if constexpr (STATS) s.c[kStatTable] += 1u;
+        } else {
+            x += ld_moff(v, row + x, pol);
+            y += ld_moff(v, row + y, pol);
+            if constexpr (STATS) s.c[kStatTable] += 2u;
+        }
     }
     const Entry *t = mic ? v.mst : v.st + static_cast<uint64_t>(lev) * v.nb;
     const uint64_t size = mic ? v.nmicro : static_cast<uint64_t>(v.levels - lev) * v.nb;
+    const bool one = MICRO && mic && x == y;
     const Entry e1 = ld_entry_keep(t, x, size, pol);
-    const Entry e2 = ld_entry_keep(t, y, size, pol);
-    if constexpr (STATS) s.c[kStatTable] += 2u;
+    Entry e2 = e1;
+    if (!one) e2 = ld_entry_keep(t, y, size, pol);
+    if constexpr (STATS) s.c[kStatTable] += one ? 1u : 2u;
     return better(e1, e2);
 }
 
@@ -747,6 +771,28 @@ __device__ __forceinline__ void flush_stats(const QStats &s, unsigned long long 
         for (int d = 16; d > 0; d >>= 1) x += __shfl_down_sync(0xffffffffu, x, d);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + c, x);
     }
+}
+
+// Answer queries [q0, q1) of one array with the whole CTA (THREADS
+// threads) in the queued form, QPT queries per thread per step; `mq` is the
+// calling warp's queue, empty on entry and on return.
+template <bool ALIGNED, bool MICRO, uint32_t MODE, int THREADS, int QPT>
+__device__ __forceinline__ void answer_range_queued(const V1View &v, const QueryOut &o,
+                                                    int64_t q0, int64_t q1, MissQueue &mq) {
+    constexpr int64_t step = static_cast<int64_t>(THREADS) * QPT;
+    QStats s;
+    uint32_t waiting = 0;
+    for (int64_t base = q0; base < q1; base += step) {
+        int2 qq[QPT];
+        load_queries<QPT>(o, base, q1, qq);
+        if (base + step <= q1)
+            answer_step_queued<ALIGNED, MICRO, MODE, THREADS, QPT, false, true>(
+                v, o, base, static_cast<uint32_t>(step), qq, s, mq, waiting);
+        else
+            answer_step_queued<ALIGNED, MICRO, MODE, THREADS, QPT, false, false>(
+                v, o, base, static_cast<uint32_t>(q1 - base), qq, s, mq, waiting);
+    }
+    if (waiting) drain_misses<MODE, false>(v, o, mq, waiting, l2_keep_policy(), s);
 }
 
 // Answer queries [q0, q1) of one array with the whole CTA, QPT queries per
