@@ -608,9 +608,8 @@ __device__ __forceinline__ uint32_t decode_bits(Entry e) {
 
 // The superset probe of the queued form for a valid query not inside one
 // micro-block: through the micro table when the query's micro-blocks fit
-// it (`mic`), else through the block table. One straight sequence: the
-// unit, level and table are selected, and only the micro table's offset
-// loads sit behind a branch.
+// it (`mic`), else through the block table (two entries, one straight
+// sequence).
 template <bool MICRO, bool STATS>
 __device__ __forceinline__ Entry superset_probe(const V1View &v, uint32_t l, uint32_t r,
                                                 uint64_t pol, QStats &s, bool &mic) {
@@ -636,14 +635,17 @@ __device__ __forceinline__ Entry superset_probe(const V1View &v, uint32_t l, uin
             y += ld_moff(v, row + y, pol);
             if constexpr (STATS) s.c[kStatTable] += 2u;
         }
+        const Entry e1 = ld_entry_keep(v.mst, x, v.nmicro, pol);
+        Entry e2 = e1;
+        if (x != y) e2 = ld_entry_keep(v.mst, y, v.nmicro, pol);
+        if constexpr (STATS) s.c[kStatTable] += x != y ? 2u : 1u;
+        return better(e1, e2);
     }
-    const Entry *t = mic ? v.mst : v.st + static_cast<uint64_t>(lev) * v.nb;
-    const uint64_t size = mic ? v.nmicro : static_cast<uint64_t>(v.levels - lev) * v.nb;
-    const bool one = MICRO && mic && x == y;
+    const Entry *t = v.st + static_cast<uint64_t>(lev) * v.nb;
+    const uint64_t size = static_cast<uint64_t>(v.levels - lev) * v.nb;
     const Entry e1 = ld_entry_keep(t, x, size, pol);
-    Entry e2 = e1;
-    if (!one) e2 = ld_entry_keep(t, y, size, pol);
-    if constexpr (STATS) s.c[kStatTable] += one ? 1u : 2u;
+    const Entry e2 = ld_entry_keep(t, y, size, pol);
+    if constexpr (STATS) s.c[kStatTable] += 2u;
     return better(e1, e2);
 }
 
