@@ -351,186 +351,32 @@ __device__ __forceinline__ uint32_t range_sectors(const V1View &v, uint32_t a, u
     return static_cast<uint32_t>(((v.off + b) >> 3) - ((v.off + a) >> 3) + 1);
 }
 
+// the probe that served a queued query (its code's low bits)
 enum : uint32_t {
-    kPathNone = 0,    // not a query of this step, or invalid
-    kPathTable,       // superset probe over blocks lB..rB
-    kPathMicroTable,  // superset probe over micro-blocks ml..mr
-    kPathMicroScan,   // inside one micro-block
-    kPathBlock,       // one block, no sub-block level
-    kPathWarpScan,    // left for the warp-cooperative scan
+    kPathTable = 1,       // superset probe over blocks lB..rB
+    kPathMicroTable = 2,  // superset probe over micro-blocks ml..mr
+    kPathBlock = 4,       // one block, no sub-block level (an edge entry settles it)
 };
 
-// One step of the CTA (the batch kernel's query phase): the QPT *
-// blockDim.x queries starting at `base`, already loaded into qq. Three
-// rounds of loads, each issued for all QPT queries of the thread before any
-// result is used: the superset probes; for the queries they do not settle,
-// the one per-element entry that is needed in any case and a narrower
-// probe; for the few still open, the rest of the three-part decomposition.
-// Uniform across the CTA (warp-cooperative scans need full warps).
-template <bool ALIGNED, int QPT, bool STATS>
-__device__ __forceinline__ void answer_step(const V1View &v, const QueryOut &o, int64_t base,
-                                            int64_t q1, const int2 (&qq)[QPT], QStats &s) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t pol = l2_keep_policy();
-    uint32_t l[QPT], r[QPT], a[QPT], b[QPT], path[QPT], side[QPT];
-    bool act[QPT];
-    Entry res[QPT], e1[QPT], e2[QPT];
-
-    // round 1: classify, probe the superset
-#pragma unroll
-    for (int k = 0; k < QPT; ++k) {
-        const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
-        act[k] = i < q1;
-        const bool ok = act[k] && qq[k].x >= 0 && qq[k].x <= qq[k].y &&
-                        static_cast<uint32_t>(qq[k].y) < v.n;
-        l[k] = ok ? static_cast<uint32_t>(qq[k].x) : 0u;
-        r[k] = ok ? static_cast<uint32_t>(qq[k].y) : 0u;
-        const uint32_t lB = div31(l[k], v.dv), rB = div31(r[k], v.dv);
-        const uint32_t ml = l[k] >> 5, mr = r[k] >> 5;
-        path[k] = kPathNone;
-        a[k] = lB;
-        b[k] = rB;
-        side[k] = 0u;
-        res[k] = kEntryNone;
-        e1[k] = kEntryNone;
-        e2[k] = kEntryNone;
-        if (ok) {
-            if (v.mst && ml == mr) {
-                path[k] = kPathMicroScan;
-            } else if (v.mst && ilog2(mr - ml + 1u) < static_cast<int>(v.mlevels)) {
-                path[k] = kPathMicroTable;
-                a[k] = ml;
-                b[k] = mr;
-            } else {
-                path[k] = lB != rB ? kPathTable : kPathBlock;
-            }
-        } else if (act[k]) {
-            if constexpr (STATS) s.c[kStatInvalid] += 1u;
-        }
-        if (path[k] == kPathTable || path[k] == kPathBlock || path[k] == kPathMicroTable)
-            res[k] = unit_probe<STATS>(v, path[k] == kPathMicroTable, a[k], b[k], pol, s);
-    }
-
-    // round 2: queries whose superset best lies outside [l, r]
-#pragma unroll
-    for (int k = 0; k < QPT; ++k) {
-        if (path[k] != kPathTable && path[k] != kPathBlock && path[k] != kPathMicroTable) continue;
-        const uint32_t m = entry_idx(res[k]);
-        if (m >= l[k] && m <= r[k]) {
-            if constexpr (STATS) s.c[kStatFirst] += 1u;
-            continue;
-        }
-        if (path[k] == kPathBlock) {
-            // one block without the sub-block level: its suffix entry at l is
-            // exact when r ends the block, its prefix entry at r when l starts it
-            const uint32_t bstart = a[k] * v.bs;
-            const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
-            if (r[k] == bend) {
-                res[k] = left_entry<STATS>(v, false, l[k], s);
-            } else if (l[k] == bstart) {
-                res[k] = right_entry<STATS>(v, false, r[k], s);
-            } else {
-                path[k] = kPathWarpScan;
-                continue;
-            }
-            if constexpr (STATS) s.c[kStatBlockEdge] += 1u;
-            continue;
-        }
-        const bool micro = path[k] == kPathMicroTable;
-        if (m < l[k]) {
-            side[k] = 1u;
-            e1[k] = left_entry<STATS>(v, micro, l[k], s);
-            e2[k] = unit_probe<STATS>(v, micro, a[k] + 1u, b[k], pol, s);
-        } else {
-            side[k] = 2u;
-            e1[k] = right_entry<STATS>(v, micro, r[k], s);
-            e2[k] = unit_probe<STATS>(v, micro, a[k], b[k] - 1u, pol, s);
-        }
-    }
-
-    // round 3: the narrower probe decides whether the other per-element
-    // entry and the middle units are needed
-#pragma unroll
-    for (int k = 0; k < QPT; ++k) {
-        if (!side[k]) continue;
-        const bool micro = path[k] == kPathMicroTable;
-        const uint32_t m2 = entry_idx(e2[k]);
-        if (side[k] == 1u ? m2 <= r[k] : m2 >= l[k]) {
-            res[k] = better(e1[k], e2[k]);
-            if constexpr (STATS) s.c[kStatSecond] += 1u;
-        } else {
-            const Entry mid = (b[k] - a[k] >= 2u)
-                                  ? unit_probe<STATS>(v, micro, a[k] + 1u, b[k] - 1u, pol, s)
-                                  : kEntryNone;
-            const Entry other = side[k] == 1u ? right_entry<STATS>(v, micro, r[k], s)
-                                              : left_entry<STATS>(v, micro, l[k], s);
-            res[k] = better(better(e1[k], other), mid);
-            if constexpr (STATS) s.c[kStatFull] += 1u;
-        }
-    }
-
-    // results: every query but the warp-scanned ones by its own thread, so a
-    // warp's 128-byte output line is written by one instruction (partial-line
-    // writes cost extra transactions, most of all to host memory)
-#pragma unroll
-    for (int k = 0; k < QPT; ++k) {
-        if (!act[k] || path[k] == kPathWarpScan) continue;
-        const int64_t i = base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x;
-        if (path[k] == kPathNone) {
-            put_invalid(o, i);
-            continue;
-        }
-        if (path[k] == kPathMicroScan) {
-            res[k] = thread_range_min<ALIGNED>(v, l[k], r[k], v.kmode);
-            if constexpr (STATS) {
-                s.c[kStatMicroScan] += 1u;
-                s.c[kStatSectors] += range_sectors(v, l[k], r[k]);
-            }
-        }
-        put_result(o, i, res[k], v.kmode);
-    }
-
-#pragma unroll
-    for (int k = 0; k < QPT; ++k) {
-        unsigned mask = __ballot_sync(0xffffffffu, path[k] == kPathWarpScan);
-        while (mask) {
-            const int src = __ffs(mask) - 1;
-            mask &= mask - 1u;
-            const uint32_t ls = __shfl_sync(0xffffffffu, l[k], src);
-            const uint32_t rs = __shfl_sync(0xffffffffu, r[k], src);
-            const Entry e = warp_scan_range<ALIGNED>(v, ls, rs, lane, v.kmode);
-            if (lane == src) {
-                put_result(o, base + threadIdx.x + static_cast<int64_t>(k) * blockDim.x, e,
-                           v.kmode);
-                if constexpr (STATS) {
-                    s.c[kStatWarpScan] += 1u;
-                    s.c[kStatSectors] += range_sectors(v, ls, rs);
-                }
-            }
-        }
-    }
-}
-
-// ---- the queued form (query_kernel) -----------------------------------------
+// ---- the queued form (query_kernel, batch_kernel's query phase) -------------
 //
-// answer_step settles a query that its probe leaves open inside the same
-// step, so a warp waits for the slowest lane's chain of dependent loads
-// (entry, narrower probe, then maybe the rest), and it carries every path's
-// state for every query. The queued form is specialised at compile time
-// on the key mode and on whether the index has the sub-block level, and
-// its main pass does only the superset probe: a query the probe settles is
-// stored at once; one it leaves open goes into a per-warp queue in shared
-// memory, and whenever 32 are waiting the warp settles them together, one
-// per lane (finish_miss).
+// Settling a query that its probe leaves open inside the same step would
+// make a warp wait for the slowest lane's chain of dependent loads (entry,
+// narrower probe, then maybe the rest). The queued form is specialised at
+// compile time on the key mode and on whether the index has the sub-block
+// level, and its main pass does only the superset probe: a query the probe
+// settles is stored at once; one it leaves open goes into a per-warp queue
+// in shared memory, and whenever 32 are waiting the warp settles them
+// together, one per lane (finish_miss).
 
 // code of a queued query: its path, and kMissLeft when the probe's best
 // lay left of l (else right of r)
 constexpr uint32_t kMissLeft = 8u;
 
-// Rounds 2 and 3 of answer_step for one query whose superset best lay
-// outside [l, r] (or, without the sub-block level, inside one block at an
-// edge): the per-element entry on that side and a narrower probe, then
-// only if needed the other entry and the middle units.
+// Settles one query whose superset best lay outside [l, r] (or, without
+// the sub-block level, inside one block at an edge): the per-element entry
+// on that side and a narrower probe, loaded together, then only if needed
+// the other entry and the middle units.
 template <bool STATS>
 __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32_t r,
                                              uint32_t code, uint64_t pol, QStats &s) {
@@ -795,20 +641,6 @@ __device__ __forceinline__ void answer_range_queued(const V1View &v, const Query
                 v, o, base, static_cast<uint32_t>(q1 - base), qq, s, mq, waiting);
     }
     if (waiting) drain_misses<MODE, false>(v, o, mq, waiting, l2_keep_policy(), s);
-}
-
-// Answer queries [q0, q1) of one array with the whole CTA, QPT queries per
-// thread per step.
-template <bool ALIGNED, int QPT>
-__device__ __forceinline__ void answer_range(const V1View &v, const QueryOut &o, int64_t q0,
-                                             int64_t q1) {
-    const int64_t step = static_cast<int64_t>(blockDim.x) * QPT;
-    QStats s;
-    for (int64_t base = q0; base < q1; base += step) {
-        int2 qq[QPT];
-        load_queries<QPT>(o, base, q1, qq);
-        answer_step<ALIGNED, QPT, false>(v, o, base, q1, qq, s);
-    }
 }
 
 }  // namespace rmq
