@@ -60,7 +60,7 @@ typedef struct rmq_info {
     int64_t table_bytes;  /* sparse table (block minima and levels)     */
     int64_t struct_bytes; /* all device memory owned by the handle      */
     int32_t micro_levels; /* levels of the sub-block table (0 = none)   */
-    int32_t reserved;
+    int32_t light;        /* 1: light index (RMQ_BUILD_LIGHT)           */
     int64_t micro_table_bytes; /* micro-block minima + table offsets     */
     int32_t is_max;       /* 1: range maximum (RMQ_BUILD_MAX)           */
     int32_t is_int32;     /* 1: int32 elements (RMQ_BUILD_INT32)        */
@@ -77,6 +77,17 @@ typedef struct rmq_info {
                                   bits (pass an int32 buffer cast to float *).
                                   The role of HRMQ's integer constructors,
                                   hrmq/includes/RMQRMM64.h:175-178 */
+#define RMQ_BUILD_LIGHT    8u  /* light index: the block and micro-block
+                                  tables only, no per-element prefix /
+                                  suffix entries (about 1.3 instead of 32
+                                  bytes per element, a build that reads the
+                                  values once and writes ~1/25 as much); a
+                                  query the table probe leaves open scans
+                                  one 128-byte line of values per end
+                                  instead of reading an entry. Needs the
+                                  sub-block level and bs a multiple of 32,
+                                  >= 64 (bs > n is rounded up to one block).
+                                  No counterpart in the reference. */
 
 /*
  * Build the index over d_vals[0..n) with block size bs (bs <= 0: default).

@@ -72,9 +72,12 @@ class RMQIndex:
     index is used (the index refers to it, it does not copy it).
     """
 
-    def __init__(self, values, bs: int = 0, stream=None, micro: bool = True, op: str = "min"):
+    def __init__(self, values, bs: int = 0, stream=None, micro: bool = True, op: str = "min",
+                 light: bool = False):
         """values: 1-D float32 or int32 CUDA tensor; op: "min" (the
-        reference's semantics) or "max"; ties resolve to the leftmost index."""
+        reference's semantics) or "max"; ties resolve to the leftmost index.
+        light=True builds the light index (RMQ_BUILD_LIGHT: tables only, no
+        per-element entries; bs a multiple of 32, >= 64)."""
         import torch
         if values.dim() != 1 or values.dtype not in (torch.float32, torch.int32):
             raise TypeError("values must be a 1-D float32 or int32 CUDA tensor")
@@ -85,7 +88,7 @@ class RMQIndex:
         self._vdtype = values.dtype
         self._h = C.c_void_p()
         flags = ((0 if micro else 1) | (2 if op == "max" else 0) |
-                 (4 if values.dtype == torch.int32 else 0))  # RMQ_BUILD_* flags
+                 (4 if values.dtype == torch.int32 else 0) | (8 if light else 0))  # RMQ_BUILD_*
         check(lib.rmq_build_ex(_dptr(values), values.numel(), int(bs), flags,
                                _stream_handle(stream), C.byref(self._h)))
 

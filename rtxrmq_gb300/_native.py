@@ -32,12 +32,13 @@ class RMQError(RuntimeError):
 class rmq_info_t(C.Structure):
     _fields_ = [("n", C.c_int64), ("bs", C.c_int64), ("nb", C.c_int64), ("levels", C.c_int32),
                 ("aligned", C.c_int32), ("table_bytes", C.c_int64), ("struct_bytes", C.c_int64),
-                ("micro_levels", C.c_int32), ("reserved", C.c_int32),
+                ("micro_levels", C.c_int32), ("light", C.c_int32),
                 ("micro_table_bytes", C.c_int64), ("is_max", C.c_int32), ("is_int32", C.c_int32)]
 
 RMQ_BUILD_NO_MICRO = 1
 RMQ_BUILD_MAX = 2
 RMQ_BUILD_INT32 = 4
+RMQ_BUILD_LIGHT = 8
 
 
 RMQ_BATCH_BUCKETS = 32

@@ -165,7 +165,8 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     NvtxRange nvtx_range("rmq_build_ex");
     g_err[0] = '\0';
     if (!out) return set_error(RMQ_EINVAL, "rmq_build: out is NULL");
-    if (flags & ~static_cast<uint32_t>(RMQ_BUILD_NO_MICRO | RMQ_BUILD_MAX | RMQ_BUILD_INT32))
+    if (flags & ~static_cast<uint32_t>(RMQ_BUILD_NO_MICRO | RMQ_BUILD_MAX | RMQ_BUILD_INT32 |
+                                       RMQ_BUILD_LIGHT))
         return set_error(RMQ_EINVAL, "rmq_build_ex: unknown flags 0x%x", flags);
     *out = nullptr;
     if (n <= 0 || n > 0x7fffffffLL)
@@ -174,7 +175,18 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     if (reinterpret_cast<uintptr_t>(d_vals) % 4 != 0)
         return set_error(RMQ_EINVAL, "rmq_build: d_vals not 4-byte aligned");
     if (bs <= 0) bs = RMQ_DEFAULT_BS;
-    if (bs > n) bs = n;
+    const bool light = (flags & RMQ_BUILD_LIGHT) != 0;
+    if (light) {
+        // blocks on micro-block boundaries; one block of the array rounded up
+        if (bs > n) bs = (n + 31) / 32 * 32;
+        if ((flags & RMQ_BUILD_NO_MICRO) || bs < 64 || bs % 32 != 0)
+            return set_error(RMQ_EINVAL,
+                             "rmq_build_ex: a light index needs the sub-block level and a block "
+                             "size that is a multiple of 32 and at least 64 (bs=%lld)",
+                             (long long)bs);
+    } else if (bs > n) {
+        bs = n;
+    }
 
     DeviceInfo dev;
     int rc = device_info(&dev);
@@ -185,6 +197,7 @@ int rmq_build_ex(const float *d_vals, int64_t n, int64_t bs, uint32_t flags, rmq
     p.A = d_vals;
     p.n = static_cast<uint32_t>(n);
     p.bs = static_cast<uint32_t>(bs);
+    p.light = light;
     p.kmode = ((flags & RMQ_BUILD_INT32) ? kIntMin : kFloatMin) + ((flags & RMQ_BUILD_MAX) ? 1u : 0u);
     const size_t total = plan_index(p, (flags & RMQ_BUILD_NO_MICRO) != 0);
 
@@ -556,7 +569,7 @@ int rmq_info(const rmq_handle_t *h, rmq_info_t *info) {
     info->table_bytes = h->table_bytes;
     info->struct_bytes = static_cast<int64_t>(h->mem_bytes);
     info->micro_levels = static_cast<int32_t>(h->plan.mlevels);
-    info->reserved = 0;
+    info->light = h->plan.light ? 1 : 0;
     info->micro_table_bytes =
         h->plan.micro ? static_cast<int64_t>(static_cast<size_t>(h->plan.nmicro) *
                                              (sizeof(Entry) + static_cast<size_t>(h->plan.moff_bytes) *

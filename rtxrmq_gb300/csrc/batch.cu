@@ -591,6 +591,7 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
     for (int32_t i = 0; i < b->narrays; ++i) {
         const BatchArray &a = b->h_arrays[i];
         BuildPlan p;
+        std::memset(&p, 0, sizeof(p));
         p.A = d_vals + a.off;
         p.n = a.n;
         p.bs = a.bs;

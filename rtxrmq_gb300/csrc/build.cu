@@ -145,6 +145,49 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
     }
 }
 
+// Light index, one pass over the values: the minimum of every 32-element
+// micro-block (level 0 of the micro table) and, folded in with a 64-bit
+// atomic minimum, of every block (level 0 of the block table, filled with
+// all-ones before; bs a multiple of 32, so every micro-block lies in one
+// block). 8 lanes per micro-block, 4 consecutive elements per lane.
+__global__ void __launch_bounds__(256)
+micro_min_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, uint32_t per_block,
+                 Entry *mst0, Entry *bmin, uint32_t mode, bool aligned) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t sub = lane & 7u;
+    const uint32_t grp = lane >> 3;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w * 4u < nmicro;
+         w += warps) {
+        const uint32_t j = w * 4u + grp;
+        const uint32_t g0 = j * kMicro + sub * 4u;
+        uint32_t b[4];
+        if (aligned && g0 + 3u < n) {
+            const uint4 f = ld_u4(A + g0);
+            b[0] = f.x;
+            b[1] = f.y;
+            b[2] = f.z;
+            b[3] = f.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) b[k] = (g0 + k < n) ? ld_u1(A + g0 + k) : 0u;
+        }
+        Entry m = kEntryNone;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (g0 + k < n) m = better(m, make_entry(b[k], g0 + k, mode));
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) m = better(m, __shfl_xor_sync(0xffffffffu, m, o, 8));
+        if (sub == 0u && j < nmicro) {
+            mst0[j] = m;
+            const uint32_t blk = j / per_block;
+            if (rmq_chk(blk < (nmicro + per_block - 1) / per_block))
+                atomicMin(reinterpret_cast<unsigned long long *>(bmin + blk),
+                          static_cast<unsigned long long>(m));
+        }
+    }
+}
+
 std::atomic<int> g_units_per_sm[2];
 
 cudaError_t launch_levels(Entry *st, uint32_t nb, uint32_t levels, const DeviceInfo &dev,
@@ -196,7 +239,7 @@ struct Offsets {
 };
 Offsets offsets_of(const BuildPlan &p) {
     Offsets o;
-    const size_t nent = a256(sizeof(Entry) * static_cast<size_t>(p.n));
+    const size_t nent = p.light ? 0 : a256(sizeof(Entry) * static_cast<size_t>(p.n));
     o.pre = 0;
     o.suf = nent;
     o.st = 2 * nent;
@@ -225,13 +268,13 @@ size_t plan_index(BuildPlan &p, bool no_micro) {
 unsigned long long *place_index(BuildPlan &p, void *base_v) {
     char *base = static_cast<char *>(base_v);
     const Offsets o = offsets_of(p);
-    p.pre = reinterpret_cast<Entry *>(base + o.pre);
-    p.suf = reinterpret_cast<Entry *>(base + o.suf);
+    p.pre = p.light ? nullptr : reinterpret_cast<Entry *>(base + o.pre);
+    p.suf = p.light ? nullptr : reinterpret_cast<Entry *>(base + o.suf);
     p.st = reinterpret_cast<Entry *>(base + o.st);
     p.mst = p.micro ? reinterpret_cast<Entry *>(base + o.mst) : nullptr;
     p.moff = p.micro ? static_cast<void *>(base + o.moff) : nullptr;
-    p.mpre = p.micro ? reinterpret_cast<Entry *>(base + o.mpre) : nullptr;
-    p.msuf = p.micro ? reinterpret_cast<Entry *>(base + o.msuf) : nullptr;
+    p.mpre = p.micro && !p.light ? reinterpret_cast<Entry *>(base + o.mpre) : nullptr;
+    p.msuf = p.micro && !p.light ? reinterpret_cast<Entry *>(base + o.msuf) : nullptr;
     return reinterpret_cast<unsigned long long *>(base + o.counter);
 }
 
@@ -248,8 +291,24 @@ uint32_t micro_levels(uint32_t bs) {
     return st_levels(touched);
 }
 
+cudaError_t launch_build_light(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {
+    cudaError_t err = cudaMemsetAsync(p.st, 0xff, sizeof(Entry) * static_cast<size_t>(p.nb), s);
+    if (err != cudaSuccess) return err;
+    uint32_t g = (p.nmicro + 31) / 32;  // 8 warps per CTA, 4 micro-blocks per warp
+    const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
+    if (g > cap) g = cap;
+    micro_min_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.bs / kMicro, p.mst, p.st, p.kmode,
+                                       p.aligned);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    err = launch_levels(p.st, p.nb, p.levels, dev, s);
+    if (err != cudaSuccess) return err;
+    return launch_micro_levels(p, dev, s);
+}
+
 cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {
     if (p.n == 0) return cudaSuccess;
+    if (p.light) return launch_build_light(p, dev, s);
     UnitJob J;
     J.A = p.A;
     J.off = 0;

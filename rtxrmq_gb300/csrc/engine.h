@@ -97,6 +97,10 @@ struct BuildPlan {
     Entry *mpre;       // [n] leftmost minimum of A[microstart(i) .. i]
     Entry *msuf;       // [n] leftmost minimum of A[i .. microend(i)]
     uint32_t kmode;    // KeyMode: float32 / int32 elements, minimum / maximum
+    // light index (RMQ_BUILD_LIGHT): the tables only, no per-element entries
+    // (pre, suf, mpre, msuf are null); needs the sub-block level and blocks
+    // on micro-block boundaries (bs a multiple of 32)
+    bool light;
 };
 constexpr uint32_t kMicro = 32;
 // levels of the micro table for block size bs (0 when not applicable)
@@ -107,9 +111,9 @@ inline uint32_t micro_offset_bytes(uint32_t mlevels) {
     return mlevels <= 9 ? 1u : (mlevels <= 17 ? 2u : 4u);
 }
 
-// Fill the size fields of a plan (A, n, bs given; micro level on unless
-// `no_micro`); returns the bytes of the single allocation holding the index
-// and its invalid-query counter.
+// Fill the size fields of a plan (A, n, bs and light given; micro level on
+// unless `no_micro`); returns the bytes of the single allocation holding the
+// index and its invalid-query counter.
 size_t plan_index(BuildPlan &p, bool no_micro);
 // Point the plan's arrays into that allocation; returns the counter.
 unsigned long long *place_index(BuildPlan &p, void *base);

@@ -20,8 +20,9 @@ namespace {
 
 constexpr char kMagic[16] = "RTXRMQ-GB300-IX";
 // 2: entries are comparison composites; 3: sub-block level for every
-// bs >= 64; 4: micro-table levels 1.. stored as offsets
-constexpr uint32_t kVersion = 4;
+// bs >= 64; 4: micro-table levels 1.. stored as offsets; 5: micro table
+// deep enough for every micro-block a block touches, light indexes
+constexpr uint32_t kVersion = 5;
 constexpr size_t kIoChunk = size_t(64) << 20;
 
 struct FileHeader {
@@ -121,7 +122,7 @@ int rmq_save(const rmq_handle_t *h, const char *path, rmq_stream_t stream) {
     std::memcpy(hd.magic, kMagic, sizeof(kMagic));
     hd.version = kVersion;
     hd.flags = (p.micro ? 0u : RMQ_BUILD_NO_MICRO) | ((p.kmode & 1u) ? RMQ_BUILD_MAX : 0u) |
-               (p.kmode >= kIntMin ? RMQ_BUILD_INT32 : 0u);
+               (p.kmode >= kIntMin ? RMQ_BUILD_INT32 : 0u) | (p.light ? RMQ_BUILD_LIGHT : 0u);
     hd.n = p.n;
     hd.bs = p.bs;
     hd.nb = p.nb;
@@ -185,7 +186,10 @@ int rmq_load(const float *d_vals, int64_t n, const char *path, rmq_stream_t stre
     p.n = static_cast<uint32_t>(n);
     p.bs = static_cast<uint32_t>(hd.bs);
     p.kmode = ((hd.flags & RMQ_BUILD_INT32) ? kIntMin : kFloatMin) + ((hd.flags & RMQ_BUILD_MAX) ? 1u : 0u);
-    const size_t bytes = (hd.bs >= 1 && hd.bs <= hd.n)
+    p.light = (hd.flags & RMQ_BUILD_LIGHT) != 0;
+    // a light index may round a block size above n up to a multiple of 32
+    const uint64_t bs_max = p.light ? (hd.n + 31) / 32 * 32 : hd.n;
+    const size_t bytes = (hd.bs >= 1 && hd.bs <= bs_max)
                              ? plan_index(p, (hd.flags & RMQ_BUILD_NO_MICRO) != 0) : 0;
     if (!bytes || bytes != hd.bytes || p.nb != hd.nb || p.levels != hd.levels ||
         p.nmicro != hd.nmicro || p.mlevels != hd.mlevels) {

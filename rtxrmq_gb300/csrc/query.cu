@@ -73,7 +73,7 @@ query_kernel(V1View v, QueryOut o, int64_t q, unsigned long long *stats) {
 #pragma unroll
         for (int k = 0; k < kQPT; ++k) cur[k] = nxt[k];
     }
-    if (waiting) drain_misses<MODE, STATS>(v, o, mq, waiting, l2_keep_policy(), s);
+    if (waiting) drain_misses<ALIGNED, MICRO, MODE, STATS>(v, o, mq, waiting, l2_keep_policy(), s);
     if constexpr (STATS) flush_stats(s, stats);
 }
 

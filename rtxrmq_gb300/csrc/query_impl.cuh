@@ -373,11 +373,40 @@ enum : uint32_t {
 // lay left of l (else right of r)
 constexpr uint32_t kMissLeft = 8u;
 
+// The part of a query in its end unit on the left, [l, end of l's unit]
+// (micro-block, or block a), and on the right, [start of r's unit, r]. With
+// per-element entries one entry each; in a light index (no entries) one
+// line of values inside the end micro-block, plus the micro table over the
+// block's whole micro-blocks for a block part.
+template <bool ALIGNED, uint32_t MODE, bool STATS>
+__device__ __forceinline__ Entry left_part(const V1View &v, bool micro, uint32_t a, uint32_t l,
+                                           uint64_t pol, QStats &s) {
+    if (v.msuf || !v.mst) return left_entry<STATS>(v, micro, l, s);
+    const uint32_t ml = l >> 5;
+    const uint32_t end = min(ml * 32u + 31u, v.n - 1u);
+    const Entry line = thread_range_min<ALIGNED>(v, l, end, MODE);
+    if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, l, end);
+    if (micro) return line;
+    const uint32_t me = (((a + 1u) * v.bs) >> 5) - 1u;  // block a is full: a < b
+    return ml < me ? better(line, micro_probe<STATS>(v, ml + 1u, me, pol, s)) : line;
+}
+template <bool ALIGNED, uint32_t MODE, bool STATS>
+__device__ __forceinline__ Entry right_part(const V1View &v, bool micro, uint32_t b, uint32_t r,
+                                            uint64_t pol, QStats &s) {
+    if (v.mpre || !v.mst) return right_entry<STATS>(v, micro, r, s);
+    const uint32_t mr = r >> 5;
+    const Entry line = thread_range_min<ALIGNED>(v, mr * 32u, r, MODE);
+    if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, mr * 32u, r);
+    if (micro) return line;
+    const uint32_t ms = (b * v.bs) >> 5;
+    return ms < mr ? better(micro_probe<STATS>(v, ms, mr - 1u, pol, s), line) : line;
+}
+
 // Settles one query whose superset best lay outside [l, r] (or, without
-// the sub-block level, inside one block at an edge): the per-element entry
-// on that side and a narrower probe, loaded together, then only if needed
-// the other entry and the middle units.
-template <bool STATS>
+// the sub-block level, inside one block at an edge): the query's part in
+// the end unit on that side and a narrower probe, loaded together, then
+// only if needed the other end's part and the middle units.
+template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
 __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32_t r,
                                              uint32_t code, uint64_t pol, QStats &s) {
     const uint32_t path = code & 7u;
@@ -391,7 +420,8 @@ __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32
     const uint32_t a = micro ? (l >> 5) : div31(l, v.dv);
     const uint32_t b = micro ? (r >> 5) : div31(r, v.dv);
     const bool left = (code & kMissLeft) != 0u;
-    const Entry e1 = left ? left_entry<STATS>(v, micro, l, s) : right_entry<STATS>(v, micro, r, s);
+    const Entry e1 = left ? left_part<ALIGNED, MODE, STATS>(v, micro, a, l, pol, s)
+                          : right_part<ALIGNED, MODE, STATS>(v, micro, b, r, pol, s);
     const Entry e2 = left ? unit_probe<STATS>(v, micro, a + 1u, b, pol, s)
                           : unit_probe<STATS>(v, micro, a, b - 1u, pol, s);
     const uint32_t m2 = entry_idx(e2);
@@ -402,7 +432,8 @@ __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32
     if constexpr (STATS) s.c[kStatFull] += 1u;
     const Entry mid = (b - a >= 2u) ? unit_probe<STATS>(v, micro, a + 1u, b - 1u, pol, s)
                                     : kEntryNone;
-    const Entry other = left ? right_entry<STATS>(v, micro, r, s) : left_entry<STATS>(v, micro, l, s);
+    const Entry other = left ? right_part<ALIGNED, MODE, STATS>(v, micro, b, r, pol, s)
+                             : left_part<ALIGNED, MODE, STATS>(v, micro, a, l, pol, s);
     return better(better(e1, other), mid);
 }
 
@@ -418,7 +449,7 @@ struct MissQueue {
 
 // Settles the last min(count, 32) queued queries, one per lane; the whole
 // warp calls it (count is warp-uniform).
-template <uint32_t MODE, bool STATS>
+template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
 __device__ __forceinline__ void drain_misses(const V1View &v, const QueryOut &o, MissQueue &mq,
                                              uint32_t &count, uint64_t pol, QStats &s) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -426,7 +457,7 @@ __device__ __forceinline__ void drain_misses(const V1View &v, const QueryOut &o,
     __syncwarp();
     if (lane < take) {
         const uint32_t e = count - take + lane;
-        const Entry r = finish_miss<STATS>(v, mq.l[e], mq.r[e], mq.code[e], pol, s);
+        const Entry r = finish_miss<ALIGNED, MICRO, MODE, STATS>(v, mq.l[e], mq.r[e], mq.code[e], pol, s);
         put_result(o, mq.qi[e], r, MODE);
     }
     __syncwarp();
@@ -585,7 +616,7 @@ __device__ __forceinline__ void answer_step_queued(const V1View &v, const QueryO
             mq.code[e] = static_cast<uint8_t>(code);
         }
         count += __popc(mask);
-        if (count >= 32u) drain_misses<MODE, STATS>(v, o, mq, count, pol, s);
+        if (count >= 32u) drain_misses<ALIGNED, MICRO, MODE, STATS>(v, o, mq, count, pol, s);
     }
     if constexpr (!MICRO) {
 #pragma unroll
@@ -640,7 +671,7 @@ __device__ __forceinline__ void answer_range_queued(const V1View &v, const Query
             answer_step_queued<ALIGNED, MICRO, MODE, THREADS, QPT, false, false>(
                 v, o, base, static_cast<uint32_t>(q1 - base), qq, s, mq, waiting);
     }
-    if (waiting) drain_misses<MODE, false>(v, o, mq, waiting, l2_keep_policy(), s);
+    if (waiting) drain_misses<ALIGNED, MICRO, MODE, false>(v, o, mq, waiting, l2_keep_policy(), s);
 }
 
 }  // namespace rmq

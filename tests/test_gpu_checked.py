@@ -86,6 +86,19 @@ for n in (1, 33, 300, 5000, 100_000, 300_001):
         assert rc == 0, rc
         eq(ni.cpu().numpy(), ei, "noalloc")
 
+# light indexes (tables only, open queries scan value lines): block sizes
+# around the micro-block and block edges, unaligned values, tie-heavy
+for n, bs, off in ((1000, 64, 0), (4097, 96, 1), (100_003, 1024, 2), (70_000, 65536, 0)):
+    A = R.gen_values_int(n, 16, n)
+    Q = R.gen_queries(20_000, n, -3, 1) if n > 2000 else np.stack(np.triu_indices(n), 1).astype(np.int32)[::7]
+    ei = oracle.base_idx(A, Q)
+    pad = np.zeros(off, np.float32)
+    big = torch.from_numpy(np.concatenate([pad, A])).to(dev)
+    with R.RMQIndex(big[off:off + n], bs, light=True) as ix:
+        v, i = ix.query(torch.from_numpy(Q).to(dev))
+        eq(i.cpu().numpy(), ei, f"light n={n} bs={bs} off={off}")
+    ran += 1
+
 # the no-allocation entry point on an index that fits its scratch only
 # without the sub-block level (the plain-index fallback)
 n = 1 << 20

@@ -1,0 +1,123 @@
+"""GPU parity of the light index (RMQ_BUILD_LIGHT: block and micro-block
+tables only, no per-element prefix / suffix entries; a query the table
+probe leaves open scans one line of values per end instead of reading an
+entry), through the C ABI, against the oracle: bit-exact values and
+leftmost indices, as for the full index."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import all_pairs, assert_matches, np_leftmost, random_case
+
+pytestmark = pytest.mark.gpu
+
+
+def run_light(cuda, A, Q, bs, op="min", off=0):
+    import torch
+
+    import rtxrmq_gb300 as R
+    pad = np.zeros(off, dtype=A.dtype)
+    big = torch.from_numpy(np.concatenate([pad, A])).to(cuda)
+    dA = big[off:off + len(A)]
+    with R.RMQIndex(dA, bs, light=True, op=op) as ix:
+        info = ix.info()
+        assert info["light"] == 1 and info["micro_levels"] > 0
+        v, i = ix.query(torch.from_numpy(np.ascontiguousarray(Q, dtype=np.int32)).to(cuda))
+        torch.cuda.synchronize()
+        return v.cpu().numpy(), i.cpu().numpy(), info
+
+
+@pytest.mark.parametrize("n", [64, 65, 95, 127, 300, 1000, 2049])
+def test_light_exhaustive_small(cuda, native, oracle_lib, n):
+    """Every (l, r) of small tie-heavy arrays for block sizes 64 .. n (and
+    one block of n rounded up to a multiple of 32)."""
+    import rtxrmq_gb300 as R
+    A = R.gen_values_int(n, 4, n + 7)
+    Q = all_pairs(n)
+    ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
+    for bs in sorted({64, 96, 128, 160, 256, 512, 1024, (n + 31) // 32 * 32}):
+        if bs > (n + 31) // 32 * 32:
+            continue
+        v, i, _ = run_light(cuda, A, Q, bs)
+        assert_matches(A, Q, v, i, ev, ei)
+
+
+@pytest.mark.parametrize("ties", [False, True])
+@pytest.mark.parametrize("lr", [-1, -2, -3, 1, 32, 1024, 65536])
+@pytest.mark.parametrize("bs", [64, 1 << 10, 1 << 13, 1 << 16])
+def test_light_length_modes(cuda, native, oracle_lib, lr, bs, ties):
+    """n=2^22 (+ a partial last block), every length mode, tie-free and
+    tie-heavy values, against the oracle's decomposition."""
+    import rtxrmq_gb300 as R
+    n, q = (1 << 22) + 1000, 1 << 15
+    A = R.gen_values_int(n, 64, 3) if ties else R.gen_values_uniform(n, 3)
+    Q = R.gen_queries(q, n, lr, 200 + lr)
+    v, i, info = run_light(cuda, A, Q, bs)
+    # no per-element entries: tables only (under 2 bytes per element here)
+    assert info["struct_bytes"] < 2 * n
+    ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
+    assert_matches(A, Q, v, i, ev, ei)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_light_random_configurations(cuda, native, seed):
+    """The parity suite's seeded random configurations (element types,
+    min / max, unaligned values, value distributions, query mixes) on the
+    light index, with the block size rounded to a multiple of 32."""
+    n, bs, dtype, op, micro, off, A, Q = random_case(seed)
+    if n < 64:
+        pytest.skip("a light index needs blocks of at least 64 elements")
+    bs = max(64, bs // 32 * 32)
+    ei = np_leftmost(A, Q, op)
+    v, i, _ = run_light(cuda, A, Q, bs, op=op, off=off)
+    bad = np.nonzero(i != ei)[0]
+    assert bad.size == 0, f"n={n} bs={bs} {dtype} {op} off={off}: first {tuple(Q[bad[0]])}"
+    np.testing.assert_array_equal(v.view(np.uint32), A[ei].view(np.uint32))
+
+
+def test_light_invalid_save_load_and_rejections(cuda, native, oracle_lib, tmp_path):
+    """Invalid queries, save / load of a light index, and the block sizes a
+    light index refuses (not a multiple of 32, below 64, no sub-block level)."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n = 100_000
+    A = R.gen_values_uniform(n, 5)
+    Q = R.gen_queries(20_000, n, -3, 6)
+    Q[:3] = [[5, 4], [0, n], [-1, 2]]
+    dA = torch.from_numpy(A).to(cuda)
+    dQ = torch.from_numpy(Q).to(cuda)
+    ei = oracle_lib.base_idx(A, Q)
+    ei[:3] = -1
+    with R.RMQIndex(dA, 2048, light=True) as ix:
+        v, i = ix.query(dQ)
+        np.testing.assert_array_equal(i.cpu().numpy(), ei)
+        assert ix.invalid_count() == 3
+        ix.save(tmp_path / "light.ix")
+        info = ix.info()
+    with R.RMQIndex.load(dA, tmp_path / "light.ix") as ix2:
+        assert ix2.info() == info
+        v2, i2 = ix2.query(dQ)
+        np.testing.assert_array_equal(i2.cpu().numpy(), ei)
+        np.testing.assert_array_equal(v2.cpu().numpy().view(np.uint32), v.cpu().numpy().view(np.uint32))
+    for bs, micro in ((100, True), (32, True), (1024, False)):
+        with pytest.raises(R.RMQError):
+            R.RMQIndex(dA, bs, light=True, micro=micro)
+
+
+@pytest.mark.parametrize("bs,lr", [(1 << 10, -3), (1 << 12, -2), (1 << 15, -1)])
+def test_light_query_stats(cuda, native, bs, lr):
+    """The counting kernel on a light index: no per-element entries are
+    read; the open queries scan value lines instead."""
+    import torch
+
+    import rtxrmq_gb300 as R
+    n, q = (1 << 22) + 77, 1 << 16
+    A = R.gen_values_uniform(n, 31)
+    Q = R.gen_queries(q, n, lr, 32)
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), bs, light=True) as ix:
+        st = ix.query_stats(torch.from_numpy(Q).to(cuda))
+    assert st["entries"] == 0
+    settled = sum(st[k] for k in ("first_probe", "second_probe", "full", "micro_scan", "invalid"))
+    assert settled == q
+    if st["second_probe"] + st["full"]:
+        assert st["scan_sectors"] > st["micro_scan"]
