@@ -38,10 +38,15 @@ __device__ __forceinline__ void load_full(const QueryOut &o, int64_t base, int2 
 // key mode and on whether the index has the sub-block level. STATS: the
 // measurement instantiation (rmq_query_stats), which also counts how each
 // query was settled and what it read into stats[kStatCount].
-template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
+template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, bool STATS>
 __global__ void __launch_bounds__(kThreads, RMQ_QUERY_MINB)
 query_kernel(V1View v, QueryOut o, int64_t q, unsigned long long *stats) {
     __shared__ MissQueue s_mq[kThreads / 32];
+    // light index only: each thread's slot for the line copies of its
+    // misses (dynamic shared memory; none is given to other launches, so
+    // they keep the whole L1)
+    extern __shared__ uint4 s_lines[];
+    uint4 *const lines = LIGHT ? s_lines : nullptr;
     constexpr int64_t chunk = static_cast<int64_t>(kThreads) * kQPT;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * chunk;
     int64_t c0 = static_cast<int64_t>(blockIdx.x) * chunk;
@@ -65,15 +70,15 @@ query_kernel(V1View v, QueryOut o, int64_t q, unsigned long long *stats) {
         else if (c1 < q)
             load_queries<kQPT>(o, c1, q, nxt);
         if (c0 <= last_full)
-            answer_step_queued<ALIGNED, MICRO, MODE, kThreads, kQPT, STATS, true>(
-                v, o, c0, static_cast<uint32_t>(chunk), cur, s, mq, waiting);
+            answer_step_queued<ALIGNED, MICRO, LIGHT, MODE, kThreads, kQPT, STATS, true>(
+                v, o, c0, static_cast<uint32_t>(chunk), cur, s, mq, waiting, lines);
         else
-            answer_step_queued<ALIGNED, MICRO, MODE, kThreads, kQPT, STATS, false>(
-                v, o, c0, static_cast<uint32_t>(q - c0), cur, s, mq, waiting);
+            answer_step_queued<ALIGNED, MICRO, LIGHT, MODE, kThreads, kQPT, STATS, false>(
+                v, o, c0, static_cast<uint32_t>(q - c0), cur, s, mq, waiting, lines);
 #pragma unroll
         for (int k = 0; k < kQPT; ++k) cur[k] = nxt[k];
     }
-    if (waiting) drain_misses<ALIGNED, MICRO, MODE, STATS>(v, o, mq, waiting, l2_keep_policy(), s);
+    if (waiting) drain_misses<ALIGNED, MICRO, LIGHT, MODE, STATS>(v, o, mq, waiting, l2_keep_policy(), s, lines);
     if constexpr (STATS) flush_stats(s, stats);
 }
 
@@ -207,27 +212,40 @@ V1View view_of(const BuildPlan &p) {
     return v;
 }
 
-template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
+constexpr size_t kLineBytes = sizeof(uint4) * kLineChunks * kThreads;  // light launches
+
+template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, bool STATS>
 cudaError_t launch_query_t(const V1View &v, const QueryOut &o, int64_t q,
                            unsigned long long *stats, const DeviceInfo &dev, cudaStream_t s) {
     static std::atomic<int> per_sm_cache{0};
-    int per_sm;
-    const cudaError_t err =
-        occupancy(query_kernel<ALIGNED, MICRO, MODE, STATS>, &per_sm_cache, &per_sm);
-    if (err != cudaSuccess) return err;
-    query_kernel<ALIGNED, MICRO, MODE, STATS>
-        <<<grid_size(q, kThreads * kQPT, per_sm, dev), kThreads, 0, s>>>(v, o, q, stats);
+    auto kern = query_kernel<ALIGNED, MICRO, LIGHT, MODE, STATS>;
+    const size_t smem = LIGHT ? kLineBytes : 0;
+    int per_sm = per_sm_cache.load(std::memory_order_relaxed);
+    if (per_sm == 0) {
+        cudaError_t err;
+        if (LIGHT) {
+            // the line slots exceed the 48 KB default of dynamic shared memory
+            err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+            if (err != cudaSuccess) return err;
+        }
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+        if (err != cudaSuccess) return err;
+        if (per_sm < 1) per_sm = 1;
+        per_sm_cache.store(per_sm, std::memory_order_relaxed);
+    }
+    kern<<<grid_size(q, kThreads * kQPT, per_sm, dev), kThreads, smem, s>>>(v, o, q, stats);
     return cudaGetLastError();
 }
 
-template <bool ALIGNED, bool MICRO, bool STATS>
+template <bool ALIGNED, bool MICRO, bool LIGHT, bool STATS>
 cudaError_t launch_query_m(const V1View &v, const QueryOut &o, int64_t q,
                            unsigned long long *stats, const DeviceInfo &dev, cudaStream_t s) {
     switch (v.kmode) {
-    case kFloatMax: return launch_query_t<ALIGNED, MICRO, kFloatMax, STATS>(v, o, q, stats, dev, s);
-    case kIntMin: return launch_query_t<ALIGNED, MICRO, kIntMin, STATS>(v, o, q, stats, dev, s);
-    case kIntMax: return launch_query_t<ALIGNED, MICRO, kIntMax, STATS>(v, o, q, stats, dev, s);
-    default: return launch_query_t<ALIGNED, MICRO, kFloatMin, STATS>(v, o, q, stats, dev, s);
+    case kFloatMax: return launch_query_t<ALIGNED, MICRO, LIGHT, kFloatMax, STATS>(v, o, q, stats, dev, s);
+    case kIntMin: return launch_query_t<ALIGNED, MICRO, LIGHT, kIntMin, STATS>(v, o, q, stats, dev, s);
+    case kIntMax: return launch_query_t<ALIGNED, MICRO, LIGHT, kIntMax, STATS>(v, o, q, stats, dev, s);
+    default: return launch_query_t<ALIGNED, MICRO, LIGHT, kFloatMin, STATS>(v, o, q, stats, dev, s);
     }
 }
 
@@ -235,11 +253,14 @@ template <bool STATS>
 cudaError_t launch_query_s(const BuildPlan &p, const V1View &v, const QueryOut &o, int64_t q,
                            unsigned long long *stats, const DeviceInfo &dev, cudaStream_t s) {
     const bool micro = v.mst != nullptr;
+    if (micro && p.light)
+        return p.aligned ? launch_query_m<true, true, true, STATS>(v, o, q, stats, dev, s)
+                         : launch_query_m<false, true, true, STATS>(v, o, q, stats, dev, s);
     if (p.aligned)
-        return micro ? launch_query_m<true, true, STATS>(v, o, q, stats, dev, s)
-                     : launch_query_m<true, false, STATS>(v, o, q, stats, dev, s);
-    return micro ? launch_query_m<false, true, STATS>(v, o, q, stats, dev, s)
-                 : launch_query_m<false, false, STATS>(v, o, q, stats, dev, s);
+        return micro ? launch_query_m<true, true, false, STATS>(v, o, q, stats, dev, s)
+                     : launch_query_m<true, false, false, STATS>(v, o, q, stats, dev, s);
+    return micro ? launch_query_m<false, true, false, STATS>(v, o, q, stats, dev, s)
+                 : launch_query_m<false, false, false, STATS>(v, o, q, stats, dev, s);
 }
 
 cudaError_t launch_query(const BuildPlan &p, const QueryArgs &a, const DeviceInfo &dev,

@@ -373,29 +373,77 @@ enum : uint32_t {
 // lay left of l (else right of r)
 constexpr uint32_t kMissLeft = 8u;
 
+// Shared-memory slot of one thread for a line of values: up to 9 16-byte
+// chunks (a 32-element micro-block not starting on a chunk boundary).
+constexpr int kLineChunks = 10;
+
+// Leftmost best of local A[lo..hi] (inside one micro-block) through an
+// asynchronous copy of the 16-byte chunks that cover it into the calling
+// thread's slot (cp.async.cg, bypassing L1), then a scan of the slot: one
+// memory round trip, few registers. The values base must be 16-byte
+// aligned; chunks past the end of the buffer are not read.
+template <uint32_t MODE>
+__device__ __forceinline__ Entry line_min_async(const V1View &v, uint32_t lo, uint32_t hi,
+                                                uint4 *slot) {
+    const int64_t glo = v.off + lo, ghi = v.off + hi;
+    const int64_t p0 = glo & ~int64_t(3);
+    const int nc = static_cast<int>(((ghi & ~int64_t(3)) - p0) / 4) + 1;
+    const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(slot));
+    for (int c = 0; c < nc; ++c) {
+        const int64_t p = p0 + 4 * c;
+        const int64_t avail = v.limit - p;  // elements of the chunk inside the buffer
+        const uint32_t bytes = avail >= 4 ? 16u : static_cast<uint32_t>(avail > 0 ? avail * 4 : 0);
+        if (rmq_chk(p >= 0 && bytes > 0u))
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                         :: "r"(sbase + 16u * c), "l"(v.A + p), "r"(bytes) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+    Entry best = kEntryNone;
+    for (int c = 0; c < nc; ++c) {
+        const uint4 f = slot[c];
+        const uint32_t w[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t g = p0 + 4 * c + k;
+            if (g >= glo && g <= ghi)
+                best = better(best, make_entry(w[k], static_cast<uint32_t>(g - v.off), MODE));
+        }
+    }
+    return best;
+}
+
+// Leftmost best of local A[lo..hi] inside one micro-block for a miss: the
+// asynchronous line copy when the thread has a slot and the values are
+// aligned, else the thread's own scan.
+template <bool ALIGNED, uint32_t MODE>
+__device__ __forceinline__ Entry line_min(const V1View &v, uint32_t lo, uint32_t hi, uint4 *slot) {
+    if (ALIGNED && slot) return line_min_async<MODE>(v, lo, hi, slot);
+    return thread_range_min<ALIGNED>(v, lo, hi, MODE);
+}
+
 // The part of a query in its end unit on the left, [l, end of l's unit]
 // (micro-block, or block a), and on the right, [start of r's unit, r]. With
 // per-element entries one entry each; in a light index (no entries) one
 // line of values inside the end micro-block, plus the micro table over the
 // block's whole micro-blocks for a block part.
-template <bool ALIGNED, uint32_t MODE, bool STATS>
+template <bool ALIGNED, bool LIGHT, uint32_t MODE, bool STATS>
 __device__ __forceinline__ Entry left_part(const V1View &v, bool micro, uint32_t a, uint32_t l,
-                                           uint64_t pol, QStats &s) {
-    if (v.msuf || !v.mst) return left_entry<STATS>(v, micro, l, s);
+                                           uint64_t pol, QStats &s, uint4 *slot) {
+    if constexpr (!LIGHT) return left_entry<STATS>(v, micro, l, s);
     const uint32_t ml = l >> 5;
     const uint32_t end = min(ml * 32u + 31u, v.n - 1u);
-    const Entry line = thread_range_min<ALIGNED>(v, l, end, MODE);
+    const Entry line = line_min<ALIGNED, MODE>(v, l, end, slot);
     if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, l, end);
     if (micro) return line;
     const uint32_t me = (((a + 1u) * v.bs) >> 5) - 1u;  // block a is full: a < b
     return ml < me ? better(line, micro_probe<STATS>(v, ml + 1u, me, pol, s)) : line;
 }
-template <bool ALIGNED, uint32_t MODE, bool STATS>
+template <bool ALIGNED, bool LIGHT, uint32_t MODE, bool STATS>
 __device__ __forceinline__ Entry right_part(const V1View &v, bool micro, uint32_t b, uint32_t r,
-                                            uint64_t pol, QStats &s) {
-    if (v.mpre || !v.mst) return right_entry<STATS>(v, micro, r, s);
+                                            uint64_t pol, QStats &s, uint4 *slot) {
+    if constexpr (!LIGHT) return right_entry<STATS>(v, micro, r, s);
     const uint32_t mr = r >> 5;
-    const Entry line = thread_range_min<ALIGNED>(v, mr * 32u, r, MODE);
+    const Entry line = line_min<ALIGNED, MODE>(v, mr * 32u, r, slot);
     if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, mr * 32u, r);
     if (micro) return line;
     const uint32_t ms = (b * v.bs) >> 5;
@@ -406,9 +454,10 @@ __device__ __forceinline__ Entry right_part(const V1View &v, bool micro, uint32_
 // the sub-block level, inside one block at an edge): the query's part in
 // the end unit on that side and a narrower probe, loaded together, then
 // only if needed the other end's part and the middle units.
-template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
+template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, bool STATS>
 __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32_t r,
-                                             uint32_t code, uint64_t pol, QStats &s) {
+                                             uint32_t code, uint64_t pol, QStats &s,
+                                             uint4 *slot) {
     const uint32_t path = code & 7u;
     if (path == kPathBlock) {
         if constexpr (STATS) s.c[kStatBlockEdge] += 1u;
@@ -420,10 +469,12 @@ __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32
     const uint32_t a = micro ? (l >> 5) : div31(l, v.dv);
     const uint32_t b = micro ? (r >> 5) : div31(r, v.dv);
     const bool left = (code & kMissLeft) != 0u;
-    const Entry e1 = left ? left_part<ALIGNED, MODE, STATS>(v, micro, a, l, pol, s)
-                          : right_part<ALIGNED, MODE, STATS>(v, micro, b, r, pol, s);
+    // the narrower probe first: its loads are in flight while the part's
+    // line is copied
     const Entry e2 = left ? unit_probe<STATS>(v, micro, a + 1u, b, pol, s)
                           : unit_probe<STATS>(v, micro, a, b - 1u, pol, s);
+    const Entry e1 = left ? left_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, a, l, pol, s, slot)
+                          : right_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, b, r, pol, s, slot);
     const uint32_t m2 = entry_idx(e2);
     if (left ? m2 <= r : m2 >= l) {
         if constexpr (STATS) s.c[kStatSecond] += 1u;
@@ -432,8 +483,8 @@ __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32
     if constexpr (STATS) s.c[kStatFull] += 1u;
     const Entry mid = (b - a >= 2u) ? unit_probe<STATS>(v, micro, a + 1u, b - 1u, pol, s)
                                     : kEntryNone;
-    const Entry other = left ? right_part<ALIGNED, MODE, STATS>(v, micro, b, r, pol, s)
-                             : left_part<ALIGNED, MODE, STATS>(v, micro, a, l, pol, s);
+    const Entry other = left ? right_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, b, r, pol, s, slot)
+                             : left_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, a, l, pol, s, slot);
     return better(better(e1, other), mid);
 }
 
@@ -449,15 +500,20 @@ struct MissQueue {
 
 // Settles the last min(count, 32) queued queries, one per lane; the whole
 // warp calls it (count is warp-uniform).
-template <bool ALIGNED, bool MICRO, uint32_t MODE, bool STATS>
+// `lines`: kLineChunks chunks of shared memory per thread of the CTA for
+// the light index's line copies, or null.
+template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, bool STATS>
 __device__ __forceinline__ void drain_misses(const V1View &v, const QueryOut &o, MissQueue &mq,
-                                             uint32_t &count, uint64_t pol, QStats &s) {
+                                             uint32_t &count, uint64_t pol, QStats &s,
+                                             uint4 *lines) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t take = count < 32u ? count : 32u;
     __syncwarp();
     if (lane < take) {
         const uint32_t e = count - take + lane;
-        const Entry r = finish_miss<ALIGNED, MICRO, MODE, STATS>(v, mq.l[e], mq.r[e], mq.code[e], pol, s);
+        const Entry r = finish_miss<ALIGNED, MICRO, LIGHT, MODE, STATS>(
+            v, mq.l[e], mq.r[e], mq.code[e], pol, s,
+            lines ? lines + threadIdx.x * kLineChunks : nullptr);
         put_result(o, mq.qi[e], r, MODE);
     }
     __syncwarp();
@@ -531,13 +587,16 @@ __device__ __forceinline__ Entry superset_probe(const V1View &v, uint32_t l, uin
 // into qq. FULL: cnt == THREADS * QPT, so no query needs a bounds check.
 // MICRO: the index has the sub-block level (then every query inside one
 // block spans few enough micro-blocks for the micro table, and only the
-// block table serves longer ones). `count` carries the warp's queue length
+// block table serves longer ones). LIGHT: a light index (no per-element
+// entries; `lines` holds the threads' line slots). `count` carries the warp's queue length
 // from step to step; the caller drains the rest.
-template <bool ALIGNED, bool MICRO, uint32_t MODE, int THREADS, int QPT, bool STATS, bool FULL>
+template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, int THREADS, int QPT, bool STATS,
+          bool FULL>
 __device__ __forceinline__ void answer_step_queued(const V1View &v, const QueryOut &o,
                                                    int64_t base, uint32_t cnt,
                                                    const int2 (&qq)[QPT], QStats &s,
-                                                   MissQueue &mq, uint32_t &count) {
+                                                   MissQueue &mq, uint32_t &count,
+                                                   uint4 *lines = nullptr) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t pol = l2_keep_policy();
     float *const vs = o.val ? o.val + base : nullptr;
@@ -616,7 +675,7 @@ __device__ __forceinline__ void answer_step_queued(const V1View &v, const QueryO
             mq.code[e] = static_cast<uint8_t>(code);
         }
         count += __popc(mask);
-        if (count >= 32u) drain_misses<ALIGNED, MICRO, MODE, STATS>(v, o, mq, count, pol, s);
+        if (count >= 32u) drain_misses<ALIGNED, MICRO, LIGHT, MODE, STATS>(v, o, mq, count, pol, s, lines);
     }
     if constexpr (!MICRO) {
 #pragma unroll
@@ -665,13 +724,13 @@ __device__ __forceinline__ void answer_range_queued(const V1View &v, const Query
         int2 qq[QPT];
         load_queries<QPT>(o, base, q1, qq);
         if (base + step <= q1)
-            answer_step_queued<ALIGNED, MICRO, MODE, THREADS, QPT, false, true>(
+            answer_step_queued<ALIGNED, MICRO, false, MODE, THREADS, QPT, false, true>(
                 v, o, base, static_cast<uint32_t>(step), qq, s, mq, waiting);
         else
-            answer_step_queued<ALIGNED, MICRO, MODE, THREADS, QPT, false, false>(
+            answer_step_queued<ALIGNED, MICRO, false, MODE, THREADS, QPT, false, false>(
                 v, o, base, static_cast<uint32_t>(q1 - base), qq, s, mq, waiting);
     }
-    if (waiting) drain_misses<ALIGNED, MICRO, MODE, false>(v, o, mq, waiting, l2_keep_policy(), s);
+    if (waiting) drain_misses<ALIGNED, MICRO, false, MODE, false>(v, o, mq, waiting, l2_keep_policy(), s, nullptr);
 }
 
 }  // namespace rmq

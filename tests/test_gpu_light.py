@@ -52,8 +52,9 @@ def test_light_length_modes(cuda, native, oracle_lib, lr, bs, ties):
     A = R.gen_values_int(n, 64, 3) if ties else R.gen_values_uniform(n, 3)
     Q = R.gen_queries(q, n, lr, 200 + lr)
     v, i, info = run_light(cuda, A, Q, bs)
-    # no per-element entries: tables only (under 2 bytes per element here)
-    assert info["struct_bytes"] < 2 * n
+    # no per-element entries: tables only (the full index holds 32 bytes per
+    # element; the block table over 64-element blocks alone is 2.4)
+    assert info["struct_bytes"] < 4 * n
     ev, ei = oracle_lib.Blocks(A, 1 << 12).query(Q)
     assert_matches(A, Q, v, i, ev, ei)
 
