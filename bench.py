@@ -427,6 +427,21 @@ def bench_plain_mode(R, dA, n, Q, out_v, out_i, args, stream, barrier, world, de
            "achieved_gbs": acc["alg_bytes"] / (ms / 1e3) / 1e9,
            "unpruned_achieved_gbs": acc["unpruned_alg_bytes"] / (ms / 1e3) / 1e9,
            "info": ix.info()}
+    # the light index (RMQ_BUILD_LIGHT) at the same block size: tables only,
+    # its construction, size and query time beside the full index's
+    if bs % 32 == 0 and bs >= 64:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        lix = R.RMQIndex(dA, bs, light=True)
+        torch.cuda.synchronize()
+        lc_ms = (time.perf_counter() - t) * 1e3
+        lfn = lambda: lix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
+        lms = time_steps(lfn, args.steps, args.warmup, stream, barrier)
+        res["light_index"] = {"rmq_s": job_rate(q, world, lms), "ms_per_step": lms,
+                              "construction_ms": lc_ms,
+                              "index_gb": lix.info()["struct_bytes"] / 1e9,
+                              "full_index_gb": res["info"]["struct_bytes"] / 1e9}
+        lix.close()
     # random-access probes with the query kernel's grid and query stream:
     # two random 8-B lookups per query into this index's prefix / suffix
     # tables (rmq_probe_gather), and into a 4 GiB buffer (rmq_probe_random,
