@@ -78,9 +78,10 @@ __global__ void micro_level_kernel(const Entry *__restrict__ mst0, O *off, uint3
 // their totals with width-8 shuffles; results are written as two 16-byte
 // stores per lane and array, and the micro-block minimum (suffix minimum at
 // its first element) as level 0 of the micro table.
+template <uint32_t MODE>
 __global__ void __launch_bounds__(256)
 micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entry *mpre,
-                  Entry *msuf, Entry *mst0, uint32_t mode, bool aligned) {
+                  Entry *msuf, Entry *mst0, bool aligned) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t sub = lane & 7u;        // lane within its micro-block
     const uint32_t grp = lane >> 3;        // micro-block within the warp
@@ -102,7 +103,7 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
         }
         Entry p[4], q[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) p[k] = (g0 + k < n) ? make_entry(b[k], g0 + k, mode) : kEntryNone;
+        for (int k = 0; k < 4; ++k) p[k] = (g0 + k < n) ? make_entry(b[k], g0 + k, MODE) : kEntryNone;
         q[3] = p[3];
 #pragma unroll
         for (int k = 2; k >= 0; --k) q[k] = better(p[k], q[k + 1]);
@@ -149,41 +150,111 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
 // micro-block (level 0 of the micro table) and, folded in with a 64-bit
 // atomic minimum, of every block (level 0 of the block table, filled with
 // all-ones before; bs a multiple of 32, so every micro-block lies in one
-// block). 8 lanes per micro-block, 4 consecutive elements per lane.
+// block). A warp takes 16 consecutive micro-blocks per step: four 512-byte
+// rows, each lane 4 consecutive elements of every row, all four loads in
+// flight before any reduction; 8 lanes reduce one micro-block. When the 16
+// micro-blocks lie in one block (bs a multiple of 512, or away from block
+// edges) the warp folds them into that block with a single atomic.
+constexpr uint32_t kMicroPerWarp = 16;
+
+// The composite minimum of one micro-block whose 32 elements lie 4 per lane
+// on the 8 lanes of group `grp` (this lane's first element at e = base +
+// 4 sub). Composites order by (key, index), so the 32-bit keys are reduced
+// first: each lane keeps its smallest key and the first position holding
+// it, the group takes the minimum key, and the leftmost lane holding that
+// key owns the leftmost best element; its position and -0.0 flag come over
+// in one shuffle. Elements at or past n take the largest key; they lie to
+// the right of every valid element, so a tie never selects one.
+template <uint32_t MODE, bool FULL>
+__device__ __forceinline__ Entry micro_row_min(const uint32_t (&b)[4], uint32_t e, uint32_t n,
+                                               uint32_t grp, uint32_t sub) {
+    uint32_t km = (FULL || e < n) ? key_of(b[0], MODE) : 0xffffffffu;
+    uint32_t info = negzero_of(b[0], MODE) << 2;  // position | (-0.0 flag << 2)
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        const uint32_t kk = (FULL || e + k < n) ? key_of(b[k], MODE) : 0xffffffffu;
+        if (kk < km) {
+            km = kk;
+            info = static_cast<uint32_t>(k) | (negzero_of(b[k], MODE) << 2);
+        }
+    }
+    uint32_t gk = km;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) gk = min(gk, __shfl_xor_sync(0xffffffffu, gk, o, 8));
+    const uint32_t owners = (__ballot_sync(0xffffffffu, km == gk) >> (grp * 8u)) & 0xffu;
+    const uint32_t w = __ffs(owners) - 1u;
+    const uint32_t winfo = __shfl_sync(0xffffffffu, info, grp * 8u + w);
+    const uint32_t base = e - 4u * sub;
+    if (!FULL && base >= n) return kEntryNone;
+    const uint32_t idx = base + 4u * w + (winfo & 3u);
+    return (static_cast<uint64_t>(gk) << 32) | (idx << 1) | (winfo >> 2);
+}
+
+template <uint32_t MODE>
 __global__ void __launch_bounds__(256)
 micro_min_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, uint32_t per_block,
-                 Entry *mst0, Entry *bmin, uint32_t mode, bool aligned) {
+                 Entry *mst0, Entry *bmin, bool aligned) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t sub = lane & 7u;
     const uint32_t grp = lane >> 3;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w * 4u < nmicro;
-         w += warps) {
-        const uint32_t j = w * 4u + grp;
-        const uint32_t g0 = j * kMicro + sub * 4u;
-        uint32_t b[4];
-        if (aligned && g0 + 3u < n) {
-            const uint4 f = ld_u4(A + g0);
-            b[0] = f.x;
-            b[1] = f.y;
-            b[2] = f.z;
-            b[3] = f.w;
+    const uint32_t nblocks = (nmicro + per_block - 1) / per_block;
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+         w * kMicroPerWarp < nmicro; w += warps) {
+        const uint32_t j0 = w * kMicroPerWarp;
+        const uint32_t e0 = j0 * kMicro + lane * 4u;  // row 0 of this lane
+        uint32_t b[4][4];
+        Entry m[4];  // micro-block j0 + 4i + grp, on all 8 lanes of the group
+        if (aligned && (j0 + kMicroPerWarp) * kMicro <= n) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint4 f = ld_u4(A + e0 + i * 128u);
+                b[i][0] = f.x;
+                b[i][1] = f.y;
+                b[i][2] = f.z;
+                b[i][3] = f.w;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                m[i] = micro_row_min<MODE, true>(b[i], e0 + i * 128u, n, grp, sub);
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) b[k] = (g0 + k < n) ? ld_u1(A + g0 + k) : 0u;
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t g = e0 + i * 128u + k;
+                    b[i][k] = g < n ? ld_u1(A + g) : 0u;
+                }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                m[i] = micro_row_min<MODE, false>(b[i], e0 + i * 128u, n, grp, sub);
         }
-        Entry m = kEntryNone;
+        if (sub == 0u) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (g0 + k < n) m = better(m, make_entry(b[k], g0 + k, mode));
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) m = better(m, __shfl_xor_sync(0xffffffffu, m, o, 8));
-        if (sub == 0u && j < nmicro) {
-            mst0[j] = m;
-            const uint32_t blk = j / per_block;
-            if (rmq_chk(blk < (nmicro + per_block - 1) / per_block))
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t j = j0 + 4u * i + grp;
+                if (j < nmicro) mst0[j] = m[i];
+            }
+        }
+        const uint32_t jl = min(j0 + kMicroPerWarp, nmicro) - 1u;
+        if (j0 / per_block == jl / per_block) {
+            // one block: micro-blocks past nmicro hold kEntryNone, the identity
+            Entry v = better(better(m[0], m[1]), better(m[2], m[3]));
+            v = better(v, __shfl_xor_sync(0xffffffffu, v, 8));
+            v = better(v, __shfl_xor_sync(0xffffffffu, v, 16));
+            const uint32_t blk = j0 / per_block;
+            if (lane == 0u && rmq_chk(blk < nblocks))
                 atomicMin(reinterpret_cast<unsigned long long *>(bmin + blk),
-                          static_cast<unsigned long long>(m));
+                          static_cast<unsigned long long>(v));
+        } else if (sub == 0u) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t j = j0 + 4u * i + grp;
+                const uint32_t blk = j / per_block;
+                if (j < nmicro && rmq_chk(blk < nblocks))
+                    atomicMin(reinterpret_cast<unsigned long long *>(bmin + blk),
+                              static_cast<unsigned long long>(m[i]));
+            }
         }
     }
 }
@@ -294,11 +365,29 @@ uint32_t micro_levels(uint32_t bs) {
 cudaError_t launch_build_light(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t s) {
     cudaError_t err = cudaMemsetAsync(p.st, 0xff, sizeof(Entry) * static_cast<size_t>(p.nb), s);
     if (err != cudaSuccess) return err;
-    uint32_t g = (p.nmicro + 31) / 32;  // 8 warps per CTA, 4 micro-blocks per warp
+    // 8 warps per CTA, kMicroPerWarp micro-blocks per warp step
+    uint32_t g = (p.nmicro + 8 * kMicroPerWarp - 1) / (8 * kMicroPerWarp);
     const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
     if (g > cap) g = cap;
-    micro_min_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.bs / kMicro, p.mst, p.st, p.kmode,
-                                       p.aligned);
+    const uint32_t per_block = p.bs / kMicro;
+    switch (p.kmode) {
+    case kFloatMax:
+        micro_min_kernel<kFloatMax><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, per_block, p.mst, p.st,
+                                                      p.aligned);
+        break;
+    case kIntMin:
+        micro_min_kernel<kIntMin><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, per_block, p.mst, p.st,
+                                                    p.aligned);
+        break;
+    case kIntMax:
+        micro_min_kernel<kIntMax><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, per_block, p.mst, p.st,
+                                                    p.aligned);
+        break;
+    default:
+        micro_min_kernel<kFloatMin><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, per_block, p.mst, p.st,
+                                                      p.aligned);
+        break;
+    }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     err = launch_levels(p.st, p.nb, p.levels, dev, s);
@@ -348,8 +437,24 @@ cudaError_t launch_build(const BuildPlan &p, const DeviceInfo &dev, cudaStream_t
     uint32_t g = (p.nmicro + 31) / 32;  // 8 warps per CTA, 4 micro-blocks per warp
     const uint32_t cap = static_cast<uint32_t>(dev.sms) * 8u;
     if (g > cap) g = cap;
-    micro_scan_kernel<<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst, p.kmode,
-                                        p.aligned);
+    switch (p.kmode) {
+    case kFloatMax:
+        micro_scan_kernel<kFloatMax><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst,
+                                                       p.aligned);
+        break;
+    case kIntMin:
+        micro_scan_kernel<kIntMin><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst,
+                                                     p.aligned);
+        break;
+    case kIntMax:
+        micro_scan_kernel<kIntMax><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst,
+                                                     p.aligned);
+        break;
+    default:
+        micro_scan_kernel<kFloatMin><<<g, 256, 0, s>>>(p.A, p.n, p.nmicro, p.mpre, p.msuf, p.mst,
+                                                       p.aligned);
+        break;
+    }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     return launch_micro_levels(p, dev, s);

@@ -75,6 +75,40 @@ def test_light_random_configurations(cuda, native, seed):
     np.testing.assert_array_equal(v.view(np.uint32), A[ei].view(np.uint32))
 
 
+@pytest.mark.parametrize("off", [0, 1])
+def test_light_special_values(cuda, native, oracle_lib, off):
+    """Values whose micro-block minimum the build finds by key before index:
+    +-0 mixed inside micro-blocks (leftmost wins with its own sign), +-inf,
+    subnormals; int32 maximum over arrays mostly at INT_MIN (the largest
+    key, the one past-the-end elements take) with a ragged last
+    micro-block; aligned and unaligned values."""
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(7 + off)
+    n = 20_000 + 17
+    A = rng.standard_normal(n).astype(np.float32)
+    for val, cnt in ((0.0, 4000), (-0.0, 4000), (np.inf, 100), (-np.inf, 50), (1e-42, 100)):
+        A[rng.integers(0, n, cnt)] = val
+    Q = np.concatenate([R.gen_queries(20_000, n, L, L) for L in (1, 2, 9, 33, 333, 4000)] +
+                       [np.array([[0, n - 1], [n - 40, n - 1], [n - 1, n - 1]], dtype=np.int32)])
+    ev, ei = oracle_lib.base_val(A, Q), oracle_lib.base_idx(A, Q)
+    for bs in (64, 1024, 20_032):
+        v, i, _ = run_light(cuda, A, Q, bs, off=off)
+        assert_matches(A, Q, v, i, ev, ei)
+    # zeros only: every answer is the leftmost element, with its own sign
+    Z = np.where(rng.random(1000 + 5) < 0.5, np.float32(0.0), np.float32(-0.0)).astype(np.float32)
+    Qz = all_pairs(len(Z))
+    v, i, _ = run_light(cuda, Z, Qz, 64, off=off)
+    np.testing.assert_array_equal(i, Qz[:, 0])
+    np.testing.assert_array_equal(v.view(np.uint32), Z[Qz[:, 0]].view(np.uint32))
+    # int32 maximum, values mostly INT_MIN: ties at the largest key
+    I = np.full(1000 + 13, np.iinfo(np.int32).min, dtype=np.int32)
+    I[rng.integers(0, len(I), 20)] = rng.integers(-5, 5, 20)
+    Qi = all_pairs(len(I))
+    v, i, _ = run_light(cuda, I, Qi, 96, op="max", off=off)
+    np.testing.assert_array_equal(i, np_leftmost(I, Qi, "max"))
+    np.testing.assert_array_equal(v, I[i])
+
+
 def test_light_invalid_save_load_and_rejections(cuda, native, oracle_lib, tmp_path):
     """Invalid queries, save / load of a light index, and the block sizes a
     light index refuses (not a multiple of 32, below 64, no sub-block level)."""
