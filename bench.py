@@ -269,19 +269,43 @@ CPU_KIND = ("HRMQ restated (oracle/hrmq_port.c: balanced-parentheses RMQ of the 
             "hrmq/RMQRMM64.cpp, ties leftmost), queries on all host threads")
 
 TRAFFIC_PROFILE = ROOT / "profiles" / "query_kernel_plain_n1e8_q2e26_lr1.md"
+# the sources query_kernel is compiled from; a traffic capture holds their digest
+QUERY_SOURCES = tuple(ROOT / "rtxrmq_gb300" / "csrc" / f
+                      for f in ("query.cu", "query_impl.cuh", "common.cuh", "engine.h"))
+
+
+def query_sources_digest():
+    """SHA-256 over the query kernel's source files, in a fixed order."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in QUERY_SOURCES:
+        h.update(f.name.encode() + b"\0" + f.read_bytes() + b"\0")
+    return h.hexdigest()
 
 
 def profiled_traffic(q):
     """DRAM bytes (read + write) per query_kernel launch of q queries, from
-    the ncu capture summarised in TRAFFIC_PROFILE (its line
-    `traffic_bytes_per_query: X`, measured on this workload), or None."""
+    the ncu capture summarised in TRAFFIC_PROFILE (its lines
+    `traffic_bytes_per_query: X`, `traffic_bs: B` and
+    `traffic_sources_sha256: H`, measured on this workload), and a
+    description of it. The bytes are None when the profile is missing or was
+    captured from other kernel sources than the ones built now."""
+    fields = {}
     try:
         for line in TRAFFIC_PROFILE.read_text().splitlines():
-            if line.strip().startswith("traffic_bytes_per_query:"):
-                return float(line.split(":", 1)[1]) * q
+            key, sep, val = line.strip().partition(":")
+            if sep and key in ("traffic_bytes_per_query", "traffic_bs", "traffic_sources_sha256"):
+                fields[key] = val.strip()
     except OSError:
-        pass
-    return None
+        return None, {"source": None, "stale": "no traffic profile"}
+    info = {"source": TRAFFIC_PROFILE.name, "bs": int(fields.get("traffic_bs", 0)) or None,
+            "bytes_per_query": float(fields.get("traffic_bytes_per_query", "nan"))}
+    if fields.get("traffic_sources_sha256") != query_sources_digest():
+        info["stale"] = "query kernel sources changed since the ncu capture"
+        return None, info
+    if "traffic_bytes_per_query" not in fields:
+        return None, info
+    return info["bytes_per_query"] * q, info
 
 
 def headline_config(n, q, lr):
@@ -829,6 +853,11 @@ def main():
     h = results[name]
     achieved = h["achieved_gbs"]
     default, label, config = headline_config(n, q, lr)
+    traffic, traffic_info = profiled_traffic(q) if default else (None, None)
+    if traffic_info and traffic_info.get("bs") not in (None, h["bs"]):
+        traffic_info["note"] = (f"captured at bs={traffic_info['bs']}; this run's bs={h['bs']} "
+                                "(lr=-1 traffic is the query stream and results at every bs "
+                                "in range)")
     line = {
         "metric": f"RMQ/s {label} (values+indices)",
         "value": h["value"], "unit": "RMQ/s", "n_gpus": world, "steps": args.steps,
@@ -844,9 +873,10 @@ def main():
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
-                     # DRAM bytes captured by ncu on the headline workload only
-                     "traffic": profiled_traffic(q) if default else None,
-                     "traffic_source": TRAFFIC_PROFILE.name if default else None,
+                     # DRAM bytes captured by ncu on the headline workload only,
+                     # from the same kernel sources
+                     "traffic": traffic,
+                     "traffic_source": traffic_info,
                      "peak_kind": f"{peak_kind} copy bandwidth",
                      "kernel": "query_kernel",
                      "alg_bytes_per_launch": h["accounting"]["alg_bytes"],

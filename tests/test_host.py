@@ -275,6 +275,26 @@ def test_bench_reference_arm(oracle_lib):
     assert line["metric"] == "RMQ/s n=1000000 q=100000 lr=-1 (values+indices)"
 
 
+def test_bench_traffic_profile_digest(tmp_path):
+    """roofline.traffic comes from the committed ncu summary only while the
+    query kernel's sources are the ones it was captured from: a summary
+    with another digest (or none) gives no bytes and says why."""
+    bench = _bench_module()
+    digest = bench.query_sources_digest()
+    assert len(digest) == 64 and digest == bench.query_sources_digest()
+    prof = tmp_path / "p.md"
+    bench.TRAFFIC_PROFILE = prof
+    prof.write_text(f"x\ntraffic_bytes_per_query: 15.5\ntraffic_bs: 16384\n"
+                    f"traffic_sources_sha256: {digest}\n")
+    b, info = bench.profiled_traffic(1000)
+    assert b == 15500.0 and info["bs"] == 16384 and "stale" not in info
+    prof.write_text("traffic_bytes_per_query: 15.5\ntraffic_sources_sha256: 00\n")
+    b, info = bench.profiled_traffic(1000)
+    assert b is None and "changed" in info["stale"]
+    prof.unlink()
+    assert bench.profiled_traffic(1000) == (None, {"source": None, "stale": "no traffic profile"})
+
+
 def test_bench_query_generators():
     """bench.py's numpy inputs: queries in range with the reference's length
     modes (fixed, uniform, lognormal 0.6 / 0.3 ln n), deterministic in the
