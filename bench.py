@@ -672,6 +672,36 @@ def bench_batched(args, dev, stream, barrier):
         dms = time_steps(lambda: b.run(dV, dQ, ov, oi), args.steps, 1, stream, barrier)
     from rtxrmq_gb300.replicas import job_rate, world
     q, nr = w.total_q, world()[1]
+    # the light index on the same workload: block and micro-block tables only,
+    # its own tuned tiles; answers compared bit for bit with the full plan's
+    t = time.perf_counter()
+    lcfg = ([(max(64, args.batch_bs // 32 * 32), 0, 0)] * 32 if args.batch_bs else
+            autotune(w.starts, w.lengths, w.qstarts, w.qcounts, dV, dQ, reps=2,
+                     queries_host=w.queries, cache=None, tiles=True, light=True))
+    ltune_s = time.perf_counter() - t
+    with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, lcfg, light=True) as b:
+        linfo = b.info()
+        lfn = lambda: b.run(dV, dQ, ov, oi)  # noqa: E731
+        lms = time_steps(lfn, args.steps, args.warmup, stream, barrier)
+        lg = graph_of(lfn, stream)
+        lgms = time_steps(lg.replay, args.steps, args.warmup, stream, barrier)
+        lbms = time_steps(lambda: b.build(dV), args.steps, args.warmup, stream, barrier)
+        lqms = time_steps(lambda: b.query(dV, dQ, ov, oi), args.steps, args.warmup, stream,
+                          barrier)
+        lmatch = bool(torch.equal(i1, oi) and torch.equal(v1.view(torch.int32),
+                                                          ov.view(torch.int32)))
+        del lg
+    res["light_index"] = {
+        "batched_graph_rmq_s": job_rate(q, nr, lgms), "batched_graph_ms": lgms,
+        "batched_rmq_s": job_rate(q, nr, lms), "batched_ms": lms,
+        "build_only_ms": lbms, "query_only_ms": lqms, "autotune_s": ltune_s,
+        "workspace_gb": linfo["workspace_bytes"] / 1e9,
+        "matches_full_index": lmatch,
+        "speedup_vs_per_array": pms / lgms,
+        "bucket_tiles": {str(k): {"bs": v[0], "query_chunk": v[1], "level_chunk": v[2]}
+                         for k, v in enumerate(lcfg) if v[0]},
+        # one read of the values, 8 B per 32 elements of micro-block minima
+        "build_alg_bytes": int(w.lengths.sum()) * 4 + int(w.lengths.sum()) // 32 * 8}
     res.update({"batched_graph_rmq_s": job_rate(q, nr, gms), "batched_graph_ms": gms,
                 "batched_rmq_s": job_rate(q, nr, ms), "batched_ms": ms,
                 "per_array_rmq_s": job_rate(q, nr, pms), "per_array_ms": pms,

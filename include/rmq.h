@@ -307,11 +307,11 @@ int rmq_checked_violations(int64_t *count);
  * positions, indices array-local. Arrays and query ranges may sit anywhere
  * in their buffers (gaps allowed). An array may be empty (length 0): it has
  * no structure, and every query it owns is invalid (index -1, value NaN,
- * counted by rmq_batch_invalid_count). Arrays are grouped into size buckets
- * floor(log2 length); h_bucket_bs[bucket] (RMQ_BATCH_BUCKETS entries, or
- * NULL; <= 0 means the default: 64 below 2^17 elements, 256 above) is the
- * block size of that bucket, as chosen by
- * rmq_batch_autotune.
+ * the bits 0x7fc00000 in an int32 plan, counted by rmq_batch_invalid_count).
+ * Arrays are grouped into size buckets floor(log2 length);
+ * h_bucket_bs[bucket] (RMQ_BATCH_BUCKETS entries, or NULL; <= 0 means the
+ * default: 64 below 2^17 elements, 256 above; 4096 for a light plan) is
+ * the block size of that bucket, as chosen by rmq_batch_autotune.
  * ---------------------------------------------------------------------- */
 #define RMQ_BATCH_BUCKETS 32
 
@@ -327,6 +327,7 @@ typedef struct rmq_batch_info {
     int32_t build_items;
     int32_t query_items;
     int32_t bucket_bs[RMQ_BATCH_BUCKETS];
+    int32_t flags;            /* the plan's rmq_batch_create_ex flags     */
 } rmq_batch_info_t;
 
 /* Plan a batch (host metadata in, device workspace allocated here). */
@@ -351,12 +352,18 @@ typedef struct rmq_batch_tile {
 } rmq_batch_tile_t;
 
 /* rmq_batch_create with a tile per bucket (h_bucket_tiles: RMQ_BATCH_BUCKETS
- * entries, or NULL for the defaults). rmq_batch_create(..., bs, out) is this
- * call with tiles {bs[b], 0, 0, 0}. */
+ * entries, or NULL for the defaults) and build flags for every array of the
+ * plan: RMQ_BUILD_INT32 (d_vals holds int32 and the value outputs are int32),
+ * RMQ_BUILD_MAX (range maximum), RMQ_BUILD_LIGHT (light index per array:
+ * block and micro-block tables only; block sizes multiples of 32 and >= 64,
+ * default 4096; an array shorter than its block size gets one block of its
+ * length rounded up to a multiple of 32, at least 64). Other flags:
+ * RMQ_EINVAL. rmq_batch_create(..., bs, out) is this call with tiles
+ * {bs[b], 0, 0, 0} and flags 0. */
 int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts,
                         const int64_t *h_lengths, const int64_t *h_qstarts,
                         const int64_t *h_qcounts,
-                        const rmq_batch_tile_t *h_bucket_tiles,
+                        const rmq_batch_tile_t *h_bucket_tiles, uint32_t flags,
                         rmq_batch_t **out);
 
 /* The plan's tile per bucket (RMQ_BATCH_BUCKETS entries, defaults filled in). */
@@ -392,7 +399,7 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals,
  * d_grad_out[q] for every query q of array i (fp32 atomics, so the order of
  * additions is not deterministic). accumulate == 0 zeroes
  * d_grad_vals[0 .. values_span) first. Indices < 0 (invalid queries) are
- * skipped. No allocation.
+ * skipped. No allocation. RMQ_EINVAL for a plan of int32 values.
  */
 int rmq_batch_scatter_grad(const rmq_batch_t *b, const int32_t *d_idx,
                            const float *d_grad_out, float *d_grad_vals,
@@ -423,15 +430,16 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts,
  * block size (as rmq_batch_autotune), then with it the query-item size
  * (512 .. 8192 queries) and then the level-item size (1024 .. 16384
  * entries), each the fastest over `reps` runs of a plan holding only that
- * bucket's arrays; absent buckets get {0, 0, 0, 0}. Allocates and frees
- * temporary plans; d_val / d_idx are scratch outputs.
+ * bucket's arrays, built with `flags` (as rmq_batch_create_ex); absent
+ * buckets get {0, 0, 0, 0}. Allocates and frees temporary plans; d_val /
+ * d_idx are scratch outputs.
  */
 int rmq_batch_autotune_ex(int32_t narrays, const int64_t *h_starts,
                           const int64_t *h_lengths, const int64_t *h_qstarts,
                           const int64_t *h_qcounts, const float *d_vals,
                           const int32_t *d_queries, float *d_val,
                           int32_t *d_idx, int32_t reps, rmq_stream_t stream,
-                          rmq_batch_tile_t *h_bucket_tiles);
+                          uint32_t flags, rmq_batch_tile_t *h_bucket_tiles);
 
 /*
  * GPU power sampling around a timed region, the role of the reference's

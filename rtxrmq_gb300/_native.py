@@ -48,7 +48,8 @@ class rmq_batch_info_t(C.Structure):
     _fields_ = [("narrays", C.c_int32), ("max_levels", C.c_int32), ("values_span", C.c_int64),
                 ("queries_span", C.c_int64), ("workspace_bytes", C.c_int64),
                 ("device_bytes", C.c_int64), ("build_items", C.c_int32),
-                ("query_items", C.c_int32), ("bucket_bs", C.c_int32 * RMQ_BATCH_BUCKETS)]
+                ("query_items", C.c_int32), ("bucket_bs", C.c_int32 * RMQ_BATCH_BUCKETS),
+                ("flags", C.c_int32)]
 
 
 class rmq_batch_tile_t(C.Structure):
@@ -79,9 +80,10 @@ SIGNATURES = {
     "rmq_probe_random": (C.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "rmq_checked_violations": (C.c_int, [C.POINTER(_i64)]),
     "rmq_batch_create": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
-    "rmq_batch_create_ex": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "rmq_batch_create_ex": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, C.c_uint32, C.POINTER(_vp)]),
     "rmq_batch_tiles": (C.c_int, [_vp, _vp]),
-    "rmq_batch_autotune_ex": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp]),
+    "rmq_batch_autotune_ex": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp,
+                                        C.c_uint32, _vp]),
     "rmq_batch_run": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_run_per_array": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmq_batch_build": (C.c_int, [_vp, _vp, _vp]),

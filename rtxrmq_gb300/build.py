@@ -28,7 +28,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-fopenmp,-O3", *ARCH]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp"]
 
-LIB_CU = ["api.cu", "build.cu", "query.cu", "batch.cu", "noalloc.cu", "persist.cu"]
+LIB_CU = ["api.cu", "build.cu", "query.cu", "batch.cu", "batch_light.cu", "noalloc.cu",
+          "persist.cu"]
 LIB_CPP = ["gen.cpp", "power.cpp"]
 CLI_CPP = ["cli.cpp"]
 

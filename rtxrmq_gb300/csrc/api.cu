@@ -598,7 +598,7 @@ int rmq_checked_violations(int64_t *count) {
     if (!RMQ_CHECKED)
         return set_error(RMQ_ENOTSUP, "rmq_checked_violations: not a checked build (RMQ_CHECKED=1)");
     const unsigned long long parts[] = {violations_build(), violations_query(), violations_batch(),
-                                        violations_persist()};
+                                        violations_batch_light(), violations_persist()};
     for (unsigned long long v : parts) {
         if (v == ~0ull) return set_error(RMQ_ECUDA, "rmq_checked_violations: counter read failed");
         *count += static_cast<int64_t>(v);

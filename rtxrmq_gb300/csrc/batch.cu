@@ -1,171 +1,24 @@
 // batch.cu -- many independent arrays of uneven length and their query sets
 // answered by one persistent, cooperative launch (build + query), the same
 // work as one plain build/query launch sequence per array, the gradient
-// scatter of the differentiable range-min, and the per-size-bucket block-size
-// autotuner.
+// scatter of the differentiable range-min, and the per-size-bucket
+// autotuner. The kernels are in batch_impl.cuh; this unit instantiates the
+// full-index kernels, batch_light.cu the light-index ones.
 //
 // The reference has no batched form: rtx_rmq<T> (src/rtx.h:24-177) builds one
 // structure for one array and launches one optixLaunch per batch of queries.
-//
-// Persistent kernel, three phases separated by grid-wide barriers of a
-// cooperative launch (all CTAs are co-resident, guaranteed by the launch):
-//   A  build items (array, unit): prefix/suffix minima + block minima,
-//      build_impl.cuh, the plain builder's CTA body;
-//   B  sparse-table levels 1..L-1 of every array, one level per barrier,
-//      items (array, level, first entry, count);
-//   C  query items (array, first query, count), query_impl.cuh.
-// Work lists are built on the host once per plan, so a run allocates nothing
-// and can be captured in a CUDA graph.
-#include <cooperative_groups.h>
-
 #include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "../../include/rmq.h"
-#include "build_impl.cuh"
-#include "engine.h"
-#include "query_impl.cuh"
-
-namespace cg = cooperative_groups;
-
-// CTAs per SM the persistent batch kernel is compiled for (a register bound).
-#ifndef RMQ_BATCH_MINB
-#define RMQ_BATCH_MINB 4
-#endif
+#include "batch_impl.cuh"
 
 namespace rmq {
 namespace {
 
-constexpr int kThreads = kBuildThreads;  // phase A runs the unit builder
-constexpr int kQPT = 2;
-// default tile schedule: queries per query item, sparse-table entries per
-// level item (a plan can set both per size bucket, rmq_batch_create_ex)
-constexpr uint32_t kQueryChunk = 2048;
-constexpr uint32_t kLevelChunk = 4096;
-constexpr int kMaxLevels = 32;
-
-struct BatchArray {
-    int64_t off;    // first value in the buffer
-    int64_t qoff;   // first query
-    int64_t pre;    // workspace entry offset of pre[]; suf[] follows at pre + n
-    int64_t st;     // workspace entry offset of the sparse table
-    uint32_t n, bs, nb, levels;
-    UnitLayout U;
-    Div31 dv;
-};
-
-struct BatchParams {
-    const float *A;
-    int64_t limit;
-    const int2 *Q;
-    float *val;
-    int32_t *idx;
-    unsigned long long *invalid;
-    Entry *ws;
-    const BatchArray *arrays;
-    const uint2 *build;
-    int32_t nbuild;
-    const uint4 *lvl;
-    int32_t maxlev;
-    int32_t lvl_start[kMaxLevels + 1];
-    const uint4 *qitems;
-    int32_t nqitems;
-    int64_t total_q;  // one past the last query any array owns
-    uint32_t phases;  // bit 0 build units, bit 1 table levels, bit 2 queries
-};
-
-__device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchArray &a) {
-    V1View v;
-    v.A = P.A;
-    v.off = a.off;
-    v.limit = P.limit;
-    v.n = a.n;
-    v.bs = a.bs;
-    v.nb = a.nb;
-    v.dv = a.dv;
-    v.pre = P.ws + a.pre;
-    v.suf = P.ws + a.pre + a.n;
-    v.st = P.ws + a.st;
-    v.mst = nullptr;  // batched arrays answer same-block queries with warp scans
-    v.moff = nullptr;
-    v.moff_bytes = 0u;
-    v.nmicro = 0;
-    v.mpre = nullptr;
-    v.msuf = nullptr;
-    v.kmode = kFloatMin;
-    v.levels = a.levels;
-    v.mlevels = 0u;
-    v.micro_span = 0u;
-    return v;
-}
-
-__device__ __forceinline__ UnitJob unit_job(const BatchParams &P, uint32_t array) {
-    const BatchArray a = P.arrays[array];
-    UnitJob J;
-    J.A = P.A;
-    J.off = a.off;
-    J.limit = P.limit;
-    J.n = a.n;
-    J.bs = a.bs;
-    J.U = a.U;
-    J.dv = a.dv;
-    J.pre = P.ws + a.pre;
-    J.suf = P.ws + a.pre + a.n;
-    J.bmin = P.ws + a.st;
-    J.kmode = kFloatMin;
-    J.nb = a.nb;
-    return J;
-}
-
-template <bool ALIGNED>
-__global__ void __launch_bounds__(kThreads, RMQ_BATCH_MINB) batch_kernel(BatchParams P) {
-    __shared__ Entry stage[kStageEntries];
-    __shared__ uint64_t s_warp[kWarpSlots];
-    __shared__ uint32_t s_flag[2 * kBuildWarps];
-    cg::grid_group grid = cg::this_grid();
-
-    // A: units
-    for (int32_t it = (P.phases & 1u) ? blockIdx.x : P.nbuild; it < P.nbuild; it += gridDim.x) {
-        const uint2 w = P.build[it];
-        build_unit<ALIGNED, kFloatMin>(unit_job(P, w.x), w.y, stage, s_warp, s_flag);
-    }
-    grid.sync();
-
-    // B: sparse-table levels
-    for (int k = 1; (P.phases & 2u) && k < P.maxlev; ++k) {
-        for (int32_t it = P.lvl_start[k] + blockIdx.x; it < P.lvl_start[k + 1]; it += gridDim.x) {
-            const uint4 w = P.lvl[it];
-            const BatchArray &a = P.arrays[w.x];
-            const Entry *prev = P.ws + a.st + static_cast<int64_t>(k - 1) * a.nb;
-            Entry *cur = P.ws + a.st + static_cast<int64_t>(k) * a.nb;
-            const uint32_t half = 1u << (k - 1);
-            for (uint32_t j = w.z + threadIdx.x; j < w.z + w.w; j += kThreads)
-                if (rmq_chk(j + half < a.nb)) cur[j] = better(prev[j], prev[j + half]);
-        }
-        grid.sync();
-    }
-
-    // C: queries, in the queued form; the warps' miss queues live in the
-    // staging memory of phase A
-    static_assert(sizeof(MissQueue) * (kThreads / 32) <= sizeof(Entry) * kStageEntries,
-                  "miss queues fit the staging memory");
-    MissQueue &mq = reinterpret_cast<MissQueue *>(stage)[threadIdx.x >> 5];
-    for (int32_t it = (P.phases & 4u) ? blockIdx.x : P.nqitems; it < P.nqitems; it += gridDim.x) {
-        const uint4 w = P.qitems[it];
-        const BatchArray a = P.arrays[w.x];
-        const V1View v = batch_view(P, a);
-        QueryOut o;
-        o.Q = P.Q + a.qoff;
-        o.val = P.val ? P.val + a.qoff : nullptr;
-        o.idx = P.idx ? P.idx + a.qoff : nullptr;
-        o.invalid = P.invalid;
-        o.span = P.total_q - a.qoff;
-        answer_range_queued<ALIGNED, false, kFloatMin, kThreads, kQPT>(
-            v, o, w.y, static_cast<int64_t>(w.y) + w.z, mq);
-    }
-}
+constexpr int kThreads = kBatchThreads;
 
 // grad_vals[off(a) + idx[q]] += grad_out[q] for every query q of array a
 __global__ void __launch_bounds__(kThreads)
@@ -184,8 +37,32 @@ scatter_grad_kernel(const BatchArray *arrays, const uint4 *qitems, int32_t nqite
     }
 }
 
-std::atomic<int> g_batch_per_sm[2];
+std::atomic<int> g_batch_per_sm[8];  // full kernels: (aligned, key mode)
 
+template <bool ALIGNED, uint32_t MODE>
+cudaError_t pick_full(const void **fn, int *per_sm) {
+    *fn = reinterpret_cast<const void *>(batch_kernel<ALIGNED, MODE>);
+    return occupancy_cached(batch_kernel<ALIGNED, MODE>, kThreads,
+                            g_batch_per_sm[(ALIGNED ? 4 : 0) + MODE], *per_sm);
+}
+
+template <bool ALIGNED>
+cudaError_t full_kernel_t(uint32_t mode, const void **fn, int *per_sm) {
+    switch (mode) {
+    case kFloatMax: return pick_full<ALIGNED, kFloatMax>(fn, per_sm);
+    case kIntMin: return pick_full<ALIGNED, kIntMin>(fn, per_sm);
+    case kIntMax: return pick_full<ALIGNED, kIntMax>(fn, per_sm);
+    default: return pick_full<ALIGNED, kFloatMin>(fn, per_sm);
+    }
+}
+
+// The kernel a run of this plan launches, its dynamic shared memory and CTAs per SM.
+cudaError_t batch_kernel_for(bool light, bool aligned, uint32_t mode, const void **fn,
+                             size_t *smem, int *per_sm) {
+    if (light) return batch_light_kernel(aligned, mode, fn, smem, per_sm);
+    *smem = 0;
+    return aligned ? full_kernel_t<true>(mode, fn, per_sm) : full_kernel_t<false>(mode, fn, per_sm);
+}
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -207,6 +84,9 @@ struct rmq_batch {
     size_t mem_bytes;
     size_t ws_bytes;
     BatchParams P;       // device pointers filled, per-run fields left empty
+    uint32_t flags;      // RMQ_BUILD_INT32 / RMQ_BUILD_MAX / RMQ_BUILD_LIGHT
+    uint32_t kmode;      // KeyMode of every array
+    bool light;          // light index (block and micro-block tables only)
     int32_t bucket_bs[RMQ_BATCH_BUCKETS];
     rmq_batch_tile_t tiles[RMQ_BATCH_BUCKETS];  // block size and tile schedule per bucket
     const float *built_vals;  // values of the last build enqueued on this plan
@@ -216,11 +96,16 @@ namespace {
 
 int bucket_of(int64_t n) { return n <= 1 ? 0 : ilog2(static_cast<uint32_t>(n)); }
 
-int64_t default_bs(int64_t n) {
-    // Without autotuning: small blocks, so that a query inside one block is
-    // a short warp scan (the batched index has no sub-block level) and the
-    // sparse table does the rest; 64 below 2^17 elements, 256 above (what
-    // the autotuner picks for the ragged benchmark, within 5% of it there).
+int64_t default_bs(int64_t n, bool light) {
+    // Without autotuning, full index: small blocks, so that a query inside
+    // one block is a short warp scan (the full batched index has no
+    // sub-block level) and the sparse table does the rest; 64 below 2^17
+    // elements, 256 above (what the autotuner picks for the ragged
+    // benchmark, within 5% of it there). Light index: the micro table
+    // answers queries inside a block and settles more of them than the
+    // block table does for queries across blocks, so blocks of 4096 (the
+    // ragged benchmark's queries: 3.1 ms against 8.8 ms at 1024).
+    if (light) return 4096;
     return n < (1 << 17) ? 64 : 256;
 }
 
@@ -232,15 +117,15 @@ namespace {
 // the arrays `m`, with tile `t` for their bucket bk; <0 on failure (rc set).
 float time_bucket(const std::vector<int64_t> &s, const std::vector<int64_t> &l,
                   const std::vector<int64_t> &qs, const std::vector<int64_t> &qc, int bk,
-                  const rmq_batch_tile_t &t, const float *d_vals, const int32_t *d_queries,
-                  float *d_val, int32_t *d_idx, int32_t reps, rmq_stream_t stream,
-                  cudaEvent_t e0, cudaEvent_t e1, int &rc) {
+                  const rmq_batch_tile_t &t, uint32_t flags, const float *d_vals,
+                  const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
+                  rmq_stream_t stream, cudaEvent_t e0, cudaEvent_t e1, int &rc) {
     rmq_batch_tile_t cfg[RMQ_BATCH_BUCKETS];
     std::memset(cfg, 0, sizeof(cfg));
     cfg[bk] = t;
     rmq_batch_t *sub = nullptr;
     rc = rmq_batch_create_ex(static_cast<int32_t>(s.size()), s.data(), l.data(), qs.data(),
-                             qc.data(), cfg, &sub);
+                             qc.data(), cfg, flags, &sub);
     if (rc) return -1.f;
     rc = rmq_batch_run(sub, d_vals, d_queries, d_val, d_idx, stream);  // warm
     float ms = -1.f;
@@ -263,7 +148,7 @@ float time_bucket(const std::vector<int64_t> &s, const std::vector<int64_t> &l,
 int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
                      const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
                      const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
-                     rmq_stream_t stream, rmq_batch_tile_t *out, bool tiles) {
+                     rmq_stream_t stream, uint32_t flags, rmq_batch_tile_t *out, bool tiles) {
     NvtxRange nvtx_range("rmq_batch_autotune");
     if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts)
         return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
@@ -299,8 +184,8 @@ int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_
             if (c > 2 * maxlen && best.bs != 0) break;
             rmq_batch_tile_t t = best;
             t.bs = c;
-            const float ms = time_bucket(s, l, qs, qc, bk, t, d_vals, d_queries, d_val, d_idx,
-                                         reps, stream, e0, e1, rc);
+            const float ms = time_bucket(s, l, qs, qc, bk, t, flags, d_vals, d_queries, d_val,
+                                         d_idx, reps, stream, e0, e1, rc);
             if (rc) break;
             if (best.bs == 0 || ms < best_ms) {
                 best_ms = ms;
@@ -312,8 +197,8 @@ int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_
             if (c == best.query_chunk) continue;
             rmq_batch_tile_t t = best;
             t.query_chunk = c;
-            const float ms = time_bucket(s, l, qs, qc, bk, t, d_vals, d_queries, d_val, d_idx,
-                                         reps, stream, e0, e1, rc);
+            const float ms = time_bucket(s, l, qs, qc, bk, t, flags, d_vals, d_queries, d_val,
+                                         d_idx, reps, stream, e0, e1, rc);
             if (!rc && ms < best_ms) {
                 best_ms = ms;
                 best = t;
@@ -324,8 +209,8 @@ int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_
             if (c == best.level_chunk) continue;
             rmq_batch_tile_t t = best;
             t.level_chunk = c;
-            const float ms = time_bucket(s, l, qs, qc, bk, t, d_vals, d_queries, d_val, d_idx,
-                                         reps, stream, e0, e1, rc);
+            const float ms = time_bucket(s, l, qs, qc, bk, t, flags, d_vals, d_queries, d_val,
+                                         d_idx, reps, stream, e0, e1, rc);
             if (!rc && ms < best_ms) {
                 best_ms = ms;
                 best = t;
@@ -352,21 +237,31 @@ int rmq_batch_create(int32_t narrays, const int64_t *h_starts, const int64_t *h_
         tiles[i].level_chunk = 0;
         tiles[i].reserved = 0;
     }
-    return rmq_batch_create_ex(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, tiles, out);
+    return rmq_batch_create_ex(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, tiles, 0u, out);
 }
 
 int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
                         const int64_t *h_qstarts, const int64_t *h_qcounts,
-                        const rmq_batch_tile_t *h_bucket_tiles, rmq_batch_t **out) {
+                        const rmq_batch_tile_t *h_bucket_tiles, uint32_t flags,
+                        rmq_batch_t **out) {
     NvtxRange nvtx_range("rmq_batch_create");
     if (!out) return set_error(RMQ_EINVAL, "rmq_batch_create: out is NULL");
     *out = nullptr;
     if (narrays <= 0 || !h_starts || !h_lengths || !h_qstarts || !h_qcounts)
         return set_error(RMQ_EINVAL, "rmq_batch_create: narrays must be > 0 and arrays non-NULL");
+    if (flags & ~static_cast<uint32_t>(RMQ_BUILD_MAX | RMQ_BUILD_INT32 | RMQ_BUILD_LIGHT))
+        return set_error(RMQ_EINVAL, "rmq_batch_create: unsupported flags 0x%x", flags);
+    const bool light = (flags & RMQ_BUILD_LIGHT) != 0;
     if (h_bucket_tiles)
-        for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i)
-            if (h_bucket_tiles[i].query_chunk < 0 || h_bucket_tiles[i].level_chunk < 0)
+        for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) {
+            const rmq_batch_tile_t &t = h_bucket_tiles[i];
+            if (t.query_chunk < 0 || t.level_chunk < 0)
                 return set_error(RMQ_EINVAL, "rmq_batch_create: bucket %d has a negative chunk", i);
+            if (light && t.bs > 0 && (t.bs < 64 || t.bs % 32 != 0))
+                return set_error(RMQ_EINVAL,
+                                 "rmq_batch_create: bucket %d: a light index needs a block size "
+                                 "that is a multiple of 32 and at least 64 (bs=%d)", i, t.bs);
+        }
     DeviceInfo dev;
     int rc = device_info(&dev);
     if (rc) return rc;
@@ -379,6 +274,9 @@ int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t 
     b->limit = 0;
     b->total_q = 0;
     b->mem = nullptr;
+    b->flags = flags;
+    b->light = light;
+    b->kmode = ((flags & RMQ_BUILD_INT32) ? kIntMin : kFloatMin) + ((flags & RMQ_BUILD_MAX) ? 1u : 0u);
     for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) {
         const rmq_batch_tile_t t = h_bucket_tiles ? h_bucket_tiles[i] : rmq_batch_tile_t{0, 0, 0, 0};
         b->bucket_bs[i] = t.bs > 0 ? t.bs : 0;
@@ -393,6 +291,13 @@ int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t 
     int64_t ws_entries = 0;
     int32_t maxlev = 1;
     b->h_arrays.resize(narrays);
+    // table item: (array, kind << 16 | level, first, count) at table step `step`
+    auto add_items = [&](int step, uint32_t i, uint32_t kind, uint32_t k, uint32_t cnt,
+                         uint32_t chunk) {
+        for (uint32_t j = 0; j < cnt; j += chunk)
+            lvl[step].push_back(make_uint4(i, (kind << 16) | k, j, std::min(chunk, cnt - j)));
+        maxlev = std::max<int32_t>(maxlev, step + 1);
+    };
     for (int32_t i = 0; i < narrays; ++i) {
         const int64_t n = h_lengths[i], s = h_starts[i];
         const int64_t qs = h_qstarts[i], qc = h_qcounts[i];
@@ -406,11 +311,14 @@ int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t 
         // an empty array has no structure; its queries (if any) are invalid
         const int bk = n > 0 ? bucket_of(n) : 0;
         int64_t bs = n > 0 ? b->bucket_bs[bk] : 1;
-        if (bs <= 0) bs = default_bs(n);
+        if (bs <= 0) bs = default_bs(n, light);
         const uint32_t qchunk = static_cast<uint32_t>(b->tiles[bk].query_chunk);
         const uint32_t lchunk = static_cast<uint32_t>(b->tiles[bk].level_chunk);
-        if (bs > n) bs = n > 0 ? n : 1;
+        // light: blocks on micro-block boundaries, one block of at least 64
+        // for an array shorter than bs
+        if (bs > n) bs = n == 0 ? 1 : (light ? std::max<int64_t>(64, (n + 31) / 32 * 32) : n);
         BatchArray &a = b->h_arrays[i];
+        std::memset(&a, 0, sizeof(a));
         a.off = s;
         a.qoff = qs;
         a.n = static_cast<uint32_t>(n);
@@ -419,20 +327,50 @@ int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t 
         a.levels = a.nb > 0 ? st_levels(a.nb) : 0u;
         a.U = make_unit_layout(a.bs, a.nb);
         a.dv = make_div31(a.bs);
-        a.pre = ws_entries;
-        ws_entries += 2 * n;
         a.st = ws_entries;
         ws_entries += static_cast<int64_t>(a.nb) * a.levels;
+        if (light) {
+            a.nmicro = static_cast<uint32_t>((n + kMicro - 1) / kMicro);
+            a.mlevels = n > 0 ? micro_levels(a.bs) : 0u;
+            a.moff_bytes = a.mlevels ? micro_offset_bytes(a.mlevels) : 0u;
+            a.mst = ws_entries;
+            ws_entries += a.nmicro;
+            a.moff = ws_entries;
+            const int64_t moff_bytes = a.mlevels > 1 ? static_cast<int64_t>(a.moff_bytes) * a.nmicro *
+                                                           (a.mlevels - 1) : 0;
+            ws_entries += (moff_bytes + 7) / 8;
+            a.pre = -1;
+        } else {
+            a.pre = ws_entries;
+            ws_entries += 2 * n;
+        }
         ws_entries = (ws_entries + 31) & ~int64_t(31);  // 256-byte alignment per array
         b->limit = std::max(b->limit, s + n);
         b->total_q = std::max(b->total_q, qs + qc);
-        maxlev = std::max<int32_t>(maxlev, static_cast<int32_t>(a.levels));
-        const uint32_t nunits = unit_count(a.nb, a.U);
-        for (uint32_t u = 0; u < nunits; ++u) build.push_back(make_uint2(i, u));
-        for (uint32_t k = 1; k < a.levels; ++k) {
-            const uint32_t cnt = a.nb - (1u << k) + 1;
-            for (uint32_t j = 0; j < cnt; j += lchunk)
-                lvl[k].push_back(make_uint4(i, k, j, std::min(lchunk, cnt - j)));
+        if (light) {
+            // A: chunks of micro-blocks; B: block minima at step 1, block
+            // level k at step k + 1; the micro table's levels as tiles at
+            // step 1 (all levels from one read), or level k at step k when
+            // the tiles' halo would not fit
+            for (uint32_t c = 0; c * kLightChunk < a.nmicro; ++c) build.push_back(make_uint2(i, c));
+            if (a.nb > 0) {
+                const uint32_t pb = a.bs / kMicro;
+                add_items(1, i, kItemBlockMinima, 0, a.nb, std::max<uint32_t>(1u, lchunk / pb));
+            }
+            for (uint32_t k = 1; k < a.levels; ++k)
+                add_items(k + 1, i, kItemBlockLevel, k, a.nb - (1u << k) + 1, lchunk);
+            if (a.mlevels >= 2 && a.nmicro >= 2) {
+                if ((1u << (a.mlevels - 1)) - 1u <= kMicroHaloMax)
+                    add_items(1, i, kItemMicroTile, 0, a.nmicro, kMicroTile);
+                else
+                    for (uint32_t k = 1; k < a.mlevels && (1u << k) <= a.nmicro; ++k)
+                        add_items(k, i, kItemMicroLevel, k, a.nmicro - (1u << k) + 1, lchunk);
+            }
+        } else {
+            const uint32_t nunits = unit_count(a.nb, a.U);
+            for (uint32_t u = 0; u < nunits; ++u) build.push_back(make_uint2(i, u));
+            for (uint32_t k = 1; k < a.levels; ++k)
+                add_items(k, i, kItemBlockLevel, k, a.nb - (1u << k) + 1, lchunk);
         }
         for (int64_t j = 0; j < qc; j += qchunk)
             b->h_qitems.push_back(make_uint4(i, static_cast<uint32_t>(j),
@@ -535,17 +473,16 @@ static int launch_batch(rmq_batch_t *b, const float *d_vals, const int32_t *d_qu
     P.idx = d_idx;
     P.phases = phases;
     const bool aligned = reinterpret_cast<uintptr_t>(d_vals) % 16 == 0;
-    void *kern = aligned ? reinterpret_cast<void *>(batch_kernel<true>)
-                         : reinterpret_cast<void *>(batch_kernel<false>);
-    int per_sm;
-    cudaError_t err = aligned ? occupancy_cached(batch_kernel<true>, kThreads, g_batch_per_sm[1], per_sm)
-                              : occupancy_cached(batch_kernel<false>, kThreads, g_batch_per_sm[0], per_sm);
+    const void *kern = nullptr;
+    size_t smem = 0;
+    int per_sm = 0;
+    cudaError_t err = batch_kernel_for(b->light, aligned, b->kmode, &kern, &smem, &per_sm);
     if (err != cudaSuccess) return cuda_fail(err, who);
     // a cooperative launch needs every CTA resident
     if (per_sm < 1) return set_error(RMQ_ENOTSUP, "%s: kernel cannot be resident", who);
     const unsigned grid = static_cast<unsigned>(dev.sms * per_sm);
     void *args[] = {&P};
-    err = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, stream);
+    err = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, smem, stream);
     if (err != cudaSuccess) return cuda_fail(err, who);
     if (phases & 1u) b->built_vals = d_vals;
     return RMQ_OK;
@@ -598,18 +535,21 @@ int rmq_batch_run_per_array(rmq_batch_t *b, const float *d_vals, const int32_t *
         p.nb = a.nb;
         p.levels = a.levels;
         p.aligned = reinterpret_cast<uintptr_t>(p.A) % 16 == 0;
-        p.pre = ws + a.pre;
-        p.suf = ws + a.pre + a.n;
         p.st = ws + a.st;
-        p.micro = false;
-        p.nmicro = 0;
-        p.mlevels = 0;
-        p.mst = nullptr;
-        p.moff = nullptr;
-        p.moff_bytes = 0u;
-        p.mpre = nullptr;
-        p.msuf = nullptr;
-        p.kmode = kFloatMin;
+        p.kmode = b->kmode;
+        p.light = b->light;
+        if (b->light) {
+            // the plain light index over the plan's own workspace layout
+            p.micro = a.mlevels > 0;
+            p.nmicro = a.nmicro;
+            p.mlevels = a.mlevels;
+            p.mst = ws + a.mst;
+            p.moff = ws + a.moff;
+            p.moff_bytes = a.moff_bytes;
+        } else {
+            p.pre = ws + a.pre;
+            p.suf = ws + a.pre + a.n;
+        }
         cudaError_t err = launch_build(p, dev, stream);
         if (err != cudaSuccess) return cuda_fail(err, "rmq_batch_run_per_array: build");
         if (qcount[i] == 0) continue;
@@ -630,6 +570,8 @@ int rmq_batch_scatter_grad(const rmq_batch_t *b, const int32_t *d_idx, const flo
     NvtxRange nvtx_range("rmq_batch_scatter_grad");
     if (!b || !d_idx || !d_grad_out || !d_grad_vals)
         return set_error(RMQ_EINVAL, "rmq_batch_scatter_grad: NULL argument");
+    if (b->kmode >= kIntMin)
+        return set_error(RMQ_EINVAL, "rmq_batch_scatter_grad: the plan holds int32 values");
     DeviceInfo dev;
     int rc = device_info(&dev);
     if (rc) return rc;
@@ -657,6 +599,7 @@ int rmq_batch_info(const rmq_batch_t *b, rmq_batch_info_t *info) {
     info->build_items = b->P.nbuild;
     info->query_items = b->P.nqitems;
     info->max_levels = b->P.maxlev;
+    info->flags = static_cast<int32_t>(b->flags);
     for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) info->bucket_bs[i] = b->bucket_bs[i];
     return RMQ_OK;
 }
@@ -692,7 +635,7 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts, const int64_t *
     if (!h_bucket_bs) return set_error(RMQ_EINVAL, "rmq_batch_autotune: NULL argument");
     rmq_batch_tile_t tiles[RMQ_BATCH_BUCKETS];
     const int rc = autotune_buckets(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, d_vals,
-                                    d_queries, d_val, d_idx, reps, stream, tiles, false);
+                                    d_queries, d_val, d_idx, reps, stream, 0u, tiles, false);
     for (int i = 0; i < RMQ_BATCH_BUCKETS; ++i) h_bucket_bs[i] = rc ? 0 : tiles[i].bs;
     return rc;
 }
@@ -700,10 +643,10 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts, const int64_t *
 int rmq_batch_autotune_ex(int32_t narrays, const int64_t *h_starts, const int64_t *h_lengths,
                           const int64_t *h_qstarts, const int64_t *h_qcounts, const float *d_vals,
                           const int32_t *d_queries, float *d_val, int32_t *d_idx, int32_t reps,
-                          rmq_stream_t stream, rmq_batch_tile_t *h_bucket_tiles) {
+                          rmq_stream_t stream, uint32_t flags, rmq_batch_tile_t *h_bucket_tiles) {
     if (!h_bucket_tiles) return set_error(RMQ_EINVAL, "rmq_batch_autotune_ex: NULL argument");
     return autotune_buckets(narrays, h_starts, h_lengths, h_qstarts, h_qcounts, d_vals, d_queries,
-                            d_val, d_idx, reps, stream, h_bucket_tiles, true);
+                            d_val, d_idx, reps, stream, flags, h_bucket_tiles, true);
 }
 
 }  // extern "C"

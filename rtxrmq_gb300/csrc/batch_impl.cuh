@@ -1,0 +1,368 @@
+// batch_impl.cuh -- the persistent batch kernels, shared by batch.cu (full
+// index: per-element prefix / suffix entries) and batch_light.cu (light
+// index: block and micro-block tables only). Each translation unit
+// instantiates only its own kernels.
+//
+// Persistent kernel, three phases separated by grid-wide barriers of a
+// cooperative launch (all CTAs are co-resident, guaranteed by the launch):
+//   A  build items. Full: (array, unit) prefix/suffix minima + block minima,
+//      the plain builder's CTA body (build_impl.cuh). Light: (array, chunk)
+//      minima of 128 micro-blocks, 16 per warp;
+//   B  table items (array, kind | level, first entry, count), one step per
+//      barrier. Full: step k computes block-table level k. Light: step k
+//      computes block-table level k - 1 (level 0, the block minima, from
+//      the micro-block minima) and micro-table level k;
+//   C  query items (array, first query, count), query_impl.cuh's queued
+//      form (light: misses settle from value lines, no entries).
+// Work lists are built on the host once per plan, so a run allocates nothing
+// and can be captured in a CUDA graph.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "build_impl.cuh"
+#include "engine.h"
+#include "query_impl.cuh"
+
+// CTAs per SM the persistent batch kernels are compiled for (a register bound).
+#ifndef RMQ_BATCH_MINB
+#define RMQ_BATCH_MINB 4
+#endif
+
+namespace rmq {
+
+constexpr int kBatchThreads = kBuildThreads;  // phase A runs the unit builder
+constexpr int kBatchQPT = 2;
+// default tile schedule: queries per query item, table entries per level
+// item (a plan can set both per size bucket, rmq_batch_create_ex)
+constexpr uint32_t kQueryChunk = 2048;
+constexpr uint32_t kLevelChunk = 4096;
+constexpr int kMaxLevels = 32;
+// micro-blocks per light build item: 16 per warp of the CTA
+constexpr uint32_t kLightChunk = kMicroPerWarp * (kBatchThreads / 32);
+
+// kinds of table items (bits 16.. of the item's second word; bits 0..15
+// hold the level)
+enum : uint32_t {
+    kItemBlockLevel = 0,   // block-table level k from level k - 1
+    kItemBlockMinima = 1,  // block-table level 0 from the micro-block minima
+    kItemMicroLevel = 2,   // micro-table level k from level k - 1
+    kItemMicroTile = 3,    // every micro-table level of a tile, in shared memory
+};
+// Micro-table tiles: kMicroTile offsets per level from one read of the tile's
+// minima plus a halo of 2^(mlevels - 1) - 1 (at most kMicroHaloMax, blocks up
+// to 65536 elements; larger blocks take one item per level).
+constexpr uint32_t kMicroTile = 2048;
+constexpr uint32_t kMicroHaloMax = 2047;
+
+struct BatchArray {
+    int64_t off;    // first value in the buffer
+    int64_t qoff;   // first query
+    int64_t pre;    // workspace entry offset of pre[]; suf[] follows at pre + n (full)
+    int64_t st;     // workspace entry offset of the sparse table
+    int64_t mst;    // workspace entry offset of the micro-block minima (light)
+    int64_t moff;   // workspace entry offset of the micro-table offsets (light)
+    uint32_t n, bs, nb, levels;
+    uint32_t nmicro, mlevels, moff_bytes, pad;
+    UnitLayout U;
+    Div31 dv;
+};
+
+struct BatchParams {
+    const float *A;
+    int64_t limit;
+    const int2 *Q;
+    float *val;
+    int32_t *idx;
+    unsigned long long *invalid;
+    Entry *ws;
+    const BatchArray *arrays;
+    const uint2 *build;
+    int32_t nbuild;
+    const uint4 *lvl;
+    int32_t maxlev;   // table steps run: 1 .. maxlev - 1
+    int32_t lvl_start[kMaxLevels + 1];
+    const uint4 *qitems;
+    int32_t nqitems;
+    int64_t total_q;  // one past the last query any array owns
+    uint32_t phases;  // bit 0 build, bit 1 table levels, bit 2 queries
+};
+
+// Dynamic shared memory of a light batch CTA: the warps' miss queues, then
+// every thread's line slot (kLineChunks 16-byte chunks).
+constexpr size_t kLightQueueBytes = sizeof(MissQueue) * (kBatchThreads / 32);
+constexpr size_t kLightSmemBytes =
+    kLightQueueBytes + sizeof(uint4) * kLineChunks * static_cast<size_t>(kBatchThreads);
+static_assert(kLightQueueBytes % 16 == 0, "line slots start 16-byte aligned");
+static_assert((kMicroTile + kMicroHaloMax) * (sizeof(Entry) + sizeof(uint16_t)) <= kLightSmemBytes,
+              "a micro-table tile fits the light CTA's shared memory");
+
+// Light kernels (batch_light.cu): the instantiation for (aligned, key mode),
+// its dynamic shared memory and CTAs per SM (the dynamic-memory limit set).
+cudaError_t batch_light_kernel(bool aligned, uint32_t mode, const void **fn, size_t *smem,
+                               int *per_sm);
+
+namespace {
+
+namespace cg = cooperative_groups;
+
+template <bool LIGHT, uint32_t MODE>
+__device__ __forceinline__ V1View batch_view(const BatchParams &P, const BatchArray &a) {
+    V1View v;
+    v.A = P.A;
+    v.off = a.off;
+    v.limit = P.limit;
+    v.n = a.n;
+    v.bs = a.bs;
+    v.nb = a.nb;
+    v.dv = a.dv;
+    v.st = P.ws + a.st;
+    v.kmode = MODE;
+    v.levels = a.levels;
+    v.mpre = nullptr;
+    v.msuf = nullptr;
+    if (LIGHT) {
+        v.pre = nullptr;
+        v.suf = nullptr;
+        v.mst = P.ws + a.mst;
+        v.moff = P.ws + a.moff;
+        v.moff_bytes = a.moff_bytes;
+        v.nmicro = a.nmicro;
+        v.mlevels = a.mlevels;
+        v.micro_span = (1u << a.mlevels) - 1u;
+    } else {
+        // full batched arrays answer same-block queries with warp scans
+        v.pre = P.ws + a.pre;
+        v.suf = P.ws + a.pre + a.n;
+        v.mst = nullptr;
+        v.moff = nullptr;
+        v.moff_bytes = 0u;
+        v.nmicro = 0;
+        v.mlevels = 0u;
+        v.micro_span = 0u;
+    }
+    return v;
+}
+
+template <uint32_t MODE>
+__device__ __forceinline__ UnitJob unit_job(const BatchParams &P, uint32_t array) {
+    const BatchArray a = P.arrays[array];
+    UnitJob J;
+    J.A = P.A;
+    J.off = a.off;
+    J.limit = P.limit;
+    J.n = a.n;
+    J.bs = a.bs;
+    J.U = a.U;
+    J.dv = a.dv;
+    J.pre = P.ws + a.pre;
+    J.suf = P.ws + a.pre + a.n;
+    J.bmin = P.ws + a.st;
+    J.kmode = MODE;
+    J.nb = a.nb;
+    return J;
+}
+
+// Light phase A: minima of micro-blocks [c * kLightChunk, ...) of one array,
+// kMicroPerWarp per warp.
+template <bool ALIGNED, uint32_t MODE>
+__device__ __forceinline__ void light_chunk(const BatchParams &P, const BatchArray &a,
+                                            uint32_t c) {
+    const uint32_t j0 = c * kLightChunk + (threadIdx.x >> 5) * kMicroPerWarp;
+    if (j0 >= a.nmicro) return;  // whole warp
+    const float *A = P.A + a.off;
+    Entry m[4];
+    // whole rows inside the array, 16-byte aligned
+    if (ALIGNED && a.off % 4 == 0 && (j0 + kMicroPerWarp) * kMicroElems <= a.n)
+        micro_min_warp<MODE, true>(A, a.n, a.nmicro, j0, P.ws + a.mst, m);
+    else
+        micro_min_warp<MODE, false>(A, a.n, a.nmicro, j0, P.ws + a.mst, m);
+}
+
+// Light table step, kind kItemBlockMinima: block minima of blocks [first,
+// first + count) from the micro-block minima (bs / 32 per block): a thread
+// per block for small blocks, a warp per block otherwise.
+__device__ __forceinline__ void light_block_minima(const BatchParams &P, const BatchArray &a,
+                                                   uint32_t first, uint32_t count) {
+    const Entry *mst = P.ws + a.mst;
+    Entry *bmin = P.ws + a.st;
+    const uint32_t pb = a.bs / kMicroElems;
+    if (pb <= 16u) {
+        for (uint32_t b = first + threadIdx.x; b < first + count; b += kBatchThreads) {
+            Entry m = kEntryNone;
+            const uint32_t j1 = min(b * pb + pb, a.nmicro);
+            for (uint32_t j = b * pb; j < j1; ++j) m = better(m, mst[j]);
+            if (rmq_chk(b < a.nb)) bmin[b] = m;
+        }
+        return;
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t b = first + (threadIdx.x >> 5); b < first + count; b += kBatchThreads / 32) {
+        Entry m = kEntryNone;
+        const uint32_t j1 = min(b * pb + pb, a.nmicro);
+        for (uint32_t j = b * pb + lane; j < j1; j += 32u) m = better(m, mst[j]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = better(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0u && rmq_chk(b < a.nb)) bmin[b] = m;
+    }
+}
+
+template <class O>
+__device__ __forceinline__ void light_micro_level_w(const BatchParams &P, const BatchArray &a,
+                                                    uint32_t k, uint32_t first, uint32_t count) {
+    O *off = reinterpret_cast<O *>(P.ws + a.moff);
+    O *__restrict__ cur = off + static_cast<size_t>(k - 1) * a.nmicro;
+    const O *__restrict__ prev = off + static_cast<size_t>(k >= 2 ? k - 2 : 0) * a.nmicro;
+    for (uint32_t i = first + threadIdx.x; i < first + count; i += kBatchThreads)
+        micro_level_at(P.ws + a.mst, cur, prev, a.nmicro, k, i);
+}
+
+// Light table step, kind kItemMicroTile: every level 1 .. mlevels - 1 of the
+// micro table at positions [t0, t0 + count) (count <= kMicroTile) from one
+// read of the minima of [t0, t0 + count + halo) into shared memory. Each
+// level keeps, per position, the tile-local index of its window's best
+// micro-block (the level below's two halves compared); positions whose
+// window leaves the loaded range are dropped level by level. Two barriers
+// per level separate the reads of the level below from the overwrite.
+template <class O>
+__device__ __forceinline__ void light_micro_tile(const BatchParams &P, const BatchArray &a,
+                                                 uint32_t t0, uint32_t count,
+                                                 unsigned char *smem) {
+    constexpr uint32_t kMaxE = kMicroTile + kMicroHaloMax;
+    constexpr int kPer = (kMaxE + kBatchThreads - 1) / kBatchThreads;
+    Entry *key = reinterpret_cast<Entry *>(smem);
+    uint16_t *best = reinterpret_cast<uint16_t *>(key + kMaxE);
+    const uint32_t halo = (1u << (a.mlevels - 1)) - 1u;
+    const uint32_t e = min(t0 + count + halo, a.nmicro) - t0;  // entries loaded
+    const Entry *mst = P.ws + a.mst;
+    for (uint32_t i = threadIdx.x; i < e; i += kBatchThreads) {
+        key[i] = rmq_chk(i < kMaxE) ? mst[t0 + i] : kEntryNone;
+        best[i] = static_cast<uint16_t>(i);
+    }
+    __syncthreads();
+    O *off = reinterpret_cast<O *>(P.ws + a.moff);
+    for (uint32_t k = 1; k < a.mlevels && (1u << k) <= e; ++k) {
+        const uint32_t half = 1u << (k - 1);
+        const uint32_t valid = e - (1u << k) + 1;  // windows inside the loaded range
+        uint16_t nb[kPer];
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            const uint32_t i = threadIdx.x + r * kBatchThreads;
+            nb[r] = 0;
+            if (i < valid) {
+                const uint16_t x = best[i], y = best[i + half];
+                nb[r] = key[y] < key[x] ? y : x;
+            }
+        }
+        __syncthreads();
+        O *__restrict__ row = off + static_cast<size_t>(k - 1) * a.nmicro + t0;
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            const uint32_t i = threadIdx.x + r * kBatchThreads;
+            if (i < valid) {
+                best[i] = nb[r];
+                if (i < count) row[i] = static_cast<O>(nb[r] - i);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Phase B: table steps 1 .. maxlev - 1, a grid barrier after each. `smem`:
+// the light CTA's shared memory (micro-table tiles), null otherwise.
+template <bool LIGHT>
+__device__ __forceinline__ void table_steps(const BatchParams &P, cg::grid_group &grid,
+                                            unsigned char *smem) {
+    for (int s = 1; (P.phases & 2u) && s < P.maxlev; ++s) {
+        for (int32_t it = P.lvl_start[s] + blockIdx.x; it < P.lvl_start[s + 1]; it += gridDim.x) {
+            const uint4 w = P.lvl[it];
+            const BatchArray &a = P.arrays[w.x];
+            const uint32_t kind = w.y >> 16, k = w.y & 0xffffu;
+            if (LIGHT && kind == kItemBlockMinima) {
+                light_block_minima(P, a, w.z, w.w);
+            } else if (LIGHT && kind == kItemMicroTile) {
+                if (a.moff_bytes == 1u)
+                    light_micro_tile<uint8_t>(P, a, w.z, w.w, smem);
+                else
+                    light_micro_tile<uint16_t>(P, a, w.z, w.w, smem);
+            } else if (LIGHT && kind == kItemMicroLevel) {
+                if (a.moff_bytes == 1u)
+                    light_micro_level_w<uint8_t>(P, a, k, w.z, w.w);
+                else if (a.moff_bytes == 2u)
+                    light_micro_level_w<uint16_t>(P, a, k, w.z, w.w);
+                else
+                    light_micro_level_w<uint32_t>(P, a, k, w.z, w.w);
+            } else {
+                const Entry *__restrict__ prev = P.ws + a.st + static_cast<int64_t>(k - 1) * a.nb;
+                Entry *__restrict__ cur = P.ws + a.st + static_cast<int64_t>(k) * a.nb;
+                const uint32_t half = 1u << (k - 1);
+                for (uint32_t j = w.z + threadIdx.x; j < w.z + w.w; j += kBatchThreads)
+                    if (rmq_chk(j + half < a.nb)) cur[j] = better(prev[j], prev[j + half]);
+            }
+        }
+        grid.sync();
+    }
+}
+
+// Phase C: the query items, in the queued form.
+template <bool ALIGNED, bool LIGHT, uint32_t MODE>
+__device__ __forceinline__ void query_items(const BatchParams &P, MissQueue &mq, uint4 *lines) {
+    for (int32_t it = (P.phases & 4u) ? blockIdx.x : P.nqitems; it < P.nqitems; it += gridDim.x) {
+        const uint4 w = P.qitems[it];
+        const BatchArray a = P.arrays[w.x];
+        const V1View v = batch_view<LIGHT, MODE>(P, a);
+        QueryOut o;
+        o.Q = P.Q + a.qoff;
+        o.val = P.val ? P.val + a.qoff : nullptr;
+        o.idx = P.idx ? P.idx + a.qoff : nullptr;
+        o.invalid = P.invalid;
+        o.span = P.total_q - a.qoff;
+        answer_range_queued<ALIGNED, LIGHT, LIGHT, MODE, kBatchThreads, kBatchQPT>(
+            v, o, w.y, static_cast<int64_t>(w.y) + w.z, mq, lines);
+    }
+}
+
+// Full index: prefix / suffix entries per element, warp scans for queries
+// inside one block.
+template <bool ALIGNED, uint32_t MODE>
+__global__ void __launch_bounds__(kBatchThreads, RMQ_BATCH_MINB) batch_kernel(BatchParams P) {
+    __shared__ Entry stage[kStageEntries];
+    __shared__ uint64_t s_warp[kWarpSlots];
+    __shared__ uint32_t s_flag[2 * kBuildWarps];
+    cg::grid_group grid = cg::this_grid();
+
+    // A: units
+    for (int32_t it = (P.phases & 1u) ? blockIdx.x : P.nbuild; it < P.nbuild; it += gridDim.x) {
+        const uint2 w = P.build[it];
+        build_unit<ALIGNED, MODE>(unit_job<MODE>(P, w.x), w.y, stage, s_warp, s_flag);
+    }
+    grid.sync();
+    table_steps<false>(P, grid, nullptr);
+    // C: the warps' miss queues live in the staging memory of phase A
+    static_assert(sizeof(MissQueue) * (kBatchThreads / 32) <= sizeof(Entry) * kStageEntries,
+                  "miss queues fit the staging memory");
+    MissQueue &mq = reinterpret_cast<MissQueue *>(stage)[threadIdx.x >> 5];
+    query_items<ALIGNED, false, MODE>(P, mq, nullptr);
+}
+
+// Light index: block and micro-block tables only. Dynamic shared memory
+// (kLightSmemBytes): miss queues, then the threads' line slots.
+template <bool ALIGNED, uint32_t MODE>
+__global__ void __launch_bounds__(kBatchThreads, RMQ_BATCH_MINB) batch_kernel_light(BatchParams P) {
+    extern __shared__ __align__(16) unsigned char s_light[];
+    cg::grid_group grid = cg::this_grid();
+
+    // A: micro-block minima
+    for (int32_t it = (P.phases & 1u) ? blockIdx.x : P.nbuild; it < P.nbuild; it += gridDim.x) {
+        const uint2 w = P.build[it];
+        light_chunk<ALIGNED, MODE>(P, P.arrays[w.x], w.y);
+    }
+    grid.sync();
+    table_steps<true>(P, grid, s_light);
+    MissQueue &mq = reinterpret_cast<MissQueue *>(s_light)[threadIdx.x >> 5];
+    uint4 *lines = reinterpret_cast<uint4 *>(s_light + kLightQueueBytes);
+    query_items<ALIGNED, true, MODE>(P, mq, lines);
+}
+
+}  // namespace
+}  // namespace rmq

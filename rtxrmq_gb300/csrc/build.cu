@@ -48,28 +48,16 @@ __global__ void st_level_kernel(Entry *st, uint32_t nb, uint32_t k) {
         if (rmq_chk(j + half < nb)) cur[j] = better(prev[j], prev[j + half]);
 }
 
-// Level k >= 1 of the micro table as offsets: the window of 2^k micro-blocks
-// at i is the windows of 2^(k-1) at i and at i + 2^(k-1); each half's best
-// micro-block is found through the level below (level 0 = the minima
-// themselves), the better of the two kept as its offset from i. Unsigned
-// comparison of composites keeps the leftmost of equal minima.
+// Level k >= 1 of the micro table as offsets (micro_level_at).
 template <class O>
 __global__ void micro_level_kernel(const Entry *__restrict__ mst0, O *off, uint32_t nmicro,
                                    uint32_t k) {
-    const uint32_t half = 1u << (k - 1);
     const uint32_t cnt = nmicro - (1u << k) + 1;
     O *cur = off + static_cast<size_t>(k - 1) * nmicro;
     const O *prev = off + static_cast<size_t>(k >= 2 ? k - 2 : 0) * nmicro;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt;
-         i += gridDim.x * blockDim.x) {
-        uint32_t a = i, b = i + half;
-        if (k >= 2) {
-            a += prev[i];
-            b += prev[i + half];
-        }
-        if (rmq_chk(a < nmicro && b < nmicro && a - i < half && b - i < 2 * half))
-            cur[i] = static_cast<O>((mst0[b] < mst0[a] ? b : a) - i);
-    }
+         i += gridDim.x * blockDim.x)
+        micro_level_at(mst0, cur, prev, nmicro, k, i);
 }
 
 // Sub-block level: 8 lanes per 32-element micro-block, 4 consecutive
@@ -155,45 +143,12 @@ micro_scan_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, Entr
 // flight before any reduction; 8 lanes reduce one micro-block. When the 16
 // micro-blocks lie in one block (bs a multiple of 512, or away from block
 // edges) the warp folds them into that block with a single atomic.
-constexpr uint32_t kMicroPerWarp = 16;
-
-// The composite minimum of one micro-block whose 32 elements lie 4 per lane
-// on the 8 lanes of group `grp` (this lane's first element at e = base +
-// 4 sub). Composites order by (key, index), so the 32-bit keys are reduced
-// first: each lane keeps its smallest key and the first position holding
-// it, the group takes the minimum key, and the leftmost lane holding that
-// key owns the leftmost best element; its position and -0.0 flag come over
-// in one shuffle. Elements at or past n take the largest key; they lie to
-// the right of every valid element, so a tie never selects one.
-template <uint32_t MODE, bool FULL>
-__device__ __forceinline__ Entry micro_row_min(const uint32_t (&b)[4], uint32_t e, uint32_t n,
-                                               uint32_t grp, uint32_t sub) {
-    uint32_t km = (FULL || e < n) ? key_of(b[0], MODE) : 0xffffffffu;
-    uint32_t info = negzero_of(b[0], MODE) << 2;  // position | (-0.0 flag << 2)
-#pragma unroll
-    for (int k = 1; k < 4; ++k) {
-        const uint32_t kk = (FULL || e + k < n) ? key_of(b[k], MODE) : 0xffffffffu;
-        if (kk < km) {
-            km = kk;
-            info = static_cast<uint32_t>(k) | (negzero_of(b[k], MODE) << 2);
-        }
-    }
-    uint32_t gk = km;
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) gk = min(gk, __shfl_xor_sync(0xffffffffu, gk, o, 8));
-    const uint32_t owners = (__ballot_sync(0xffffffffu, km == gk) >> (grp * 8u)) & 0xffu;
-    const uint32_t w = __ffs(owners) - 1u;
-    const uint32_t winfo = __shfl_sync(0xffffffffu, info, grp * 8u + w);
-    const uint32_t base = e - 4u * sub;
-    if (!FULL && base >= n) return kEntryNone;
-    const uint32_t idx = base + 4u * w + (winfo & 3u);
-    return (static_cast<uint64_t>(gk) << 32) | (idx << 1) | (winfo >> 2);
-}
 
 template <uint32_t MODE>
 __global__ void __launch_bounds__(256)
 micro_min_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, uint32_t per_block,
                  Entry *mst0, Entry *bmin, bool aligned) {
+    static_assert(kMicroElems == kMicro, "micro-block size");
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t sub = lane & 7u;
     const uint32_t grp = lane >> 3;
@@ -202,40 +157,11 @@ micro_min_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, uint3
     for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
          w * kMicroPerWarp < nmicro; w += warps) {
         const uint32_t j0 = w * kMicroPerWarp;
-        const uint32_t e0 = j0 * kMicro + lane * 4u;  // row 0 of this lane
-        uint32_t b[4][4];
         Entry m[4];  // micro-block j0 + 4i + grp, on all 8 lanes of the group
-        if (aligned && (j0 + kMicroPerWarp) * kMicro <= n) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const uint4 f = ld_u4(A + e0 + i * 128u);
-                b[i][0] = f.x;
-                b[i][1] = f.y;
-                b[i][2] = f.z;
-                b[i][3] = f.w;
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                m[i] = micro_row_min<MODE, true>(b[i], e0 + i * 128u, n, grp, sub);
-        } else {
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint32_t g = e0 + i * 128u + k;
-                    b[i][k] = g < n ? ld_u1(A + g) : 0u;
-                }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                m[i] = micro_row_min<MODE, false>(b[i], e0 + i * 128u, n, grp, sub);
-        }
-        if (sub == 0u) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const uint32_t j = j0 + 4u * i + grp;
-                if (j < nmicro) mst0[j] = m[i];
-            }
-        }
+        if (aligned && (j0 + kMicroPerWarp) * kMicro <= n)
+            micro_min_warp<MODE, true>(A, n, nmicro, j0, mst0, m);
+        else
+            micro_min_warp<MODE, false>(A, n, nmicro, j0, mst0, m);
         const uint32_t jl = min(j0 + kMicroPerWarp, nmicro) - 1u;
         if (j0 / per_block == jl / per_block) {
             // one block: micro-blocks past nmicro hold kEntryNone, the identity

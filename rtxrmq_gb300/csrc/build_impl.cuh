@@ -734,4 +734,107 @@ __device__ __forceinline__ void build_unit(const UnitJob &J, uint32_t u, Entry *
     }
 }
 
+// ---- light index: micro-block minima and the micro table's levels ----
+
+constexpr uint32_t kMicroElems = 32;    // elements per micro-block
+constexpr uint32_t kMicroPerWarp = 16;  // micro-blocks a warp reduces per step
+
+// The composite minimum of one micro-block whose 32 elements lie 4 per lane
+// on the 8 lanes of group `grp` (this lane's first element at e = base +
+// 4 sub). Composites order by (key, index), so the 32-bit keys are reduced
+// first: each lane keeps its smallest key and the first position holding
+// it, the group takes the minimum key, and the leftmost lane holding that
+// key owns the leftmost best element; its position and -0.0 flag come over
+// in one shuffle. Elements at or past n take the largest key; they lie to
+// the right of every valid element, so a tie never selects one.
+template <uint32_t MODE, bool FULL>
+__device__ __forceinline__ Entry micro_row_min(const uint32_t (&b)[4], uint32_t e, uint32_t n,
+                                               uint32_t grp, uint32_t sub) {
+    uint32_t km = (FULL || e < n) ? key_of(b[0], MODE) : 0xffffffffu;
+    uint32_t info = negzero_of(b[0], MODE) << 2;  // position | (-0.0 flag << 2)
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        const uint32_t kk = (FULL || e + k < n) ? key_of(b[k], MODE) : 0xffffffffu;
+        if (kk < km) {
+            km = kk;
+            info = static_cast<uint32_t>(k) | (negzero_of(b[k], MODE) << 2);
+        }
+    }
+    uint32_t gk = km;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) gk = min(gk, __shfl_xor_sync(0xffffffffu, gk, o, 8));
+    const uint32_t owners = (__ballot_sync(0xffffffffu, km == gk) >> (grp * 8u)) & 0xffu;
+    const uint32_t w = __ffs(owners) - 1u;
+    const uint32_t winfo = __shfl_sync(0xffffffffu, info, grp * 8u + w);
+    const uint32_t base = e - 4u * sub;
+    if (!FULL && base >= n) return kEntryNone;
+    const uint32_t idx = base + 4u * w + (winfo & 3u);
+    return (static_cast<uint64_t>(gk) << 32) | (idx << 1) | (winfo >> 2);
+}
+
+// One offset of level k >= 1 of the micro table (as offsets): the window of
+// 2^k micro-blocks at i is the windows of 2^(k-1) at i and i + 2^(k-1); each
+// half's best micro-block comes from the level below (`prev`, level k - 1;
+// level 0 = the minima themselves), the better of the two is kept as its
+// offset from i in `cur`. Unsigned comparison of composites keeps the
+// leftmost of equal minima.
+template <class O>
+__device__ __forceinline__ void micro_level_at(const Entry *__restrict__ mst0, O *cur,
+                                               const O *prev, uint32_t nmicro, uint32_t k,
+                                               uint32_t i) {
+    const uint32_t half = 1u << (k - 1);
+    uint32_t a = i, b = i + half;
+    if (k >= 2) {
+        a += prev[i];
+        b += prev[i + half];
+    }
+    if (rmq_chk(a < nmicro && b < nmicro && a - i < half && b - i < 2 * half))
+        cur[i] = static_cast<O>((mst0[b] < mst0[a] ? b : a) - i);
+}
+
+// Micro-block minima of micro-blocks [j0, j0 + 16) of one array (values
+// A[0 .. n), nmicro = ceil(n / 32)) with one whole warp: four 512-byte rows,
+// each lane 4 consecutive elements of every row, all loads in flight before
+// any reduction (micro_row_min). VEC: 16-byte loads (A + j0 * 32 16-byte
+// aligned and all 512 elements inside the array). Writes mst0[j] for j <
+// nmicro; returns the four minima of the lane's group (micro-blocks j0 + 4i
+// + lane / 8; kEntryNone past nmicro).
+template <uint32_t MODE, bool VEC>
+__device__ __forceinline__ void micro_min_warp(const float *__restrict__ A, uint32_t n,
+                                               uint32_t nmicro, uint32_t j0, Entry *mst0,
+                                               Entry (&m)[4]) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t sub = lane & 7u;
+    const uint32_t grp = lane >> 3;
+    const uint32_t e0 = j0 * kMicroElems + lane * 4u;  // row 0 of this lane
+    uint32_t b[4][4];
+    if (VEC) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint4 f = ld_u4(A + e0 + i * 128u);
+            b[i][0] = f.x;
+            b[i][1] = f.y;
+            b[i][2] = f.z;
+            b[i][3] = f.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t g = e0 + i * 128u + k;
+                b[i][k] = g < n ? ld_u1(A + g) : 0u;
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) m[i] = micro_row_min<MODE, VEC>(b[i], e0 + i * 128u, n, grp, sub);
+    if (sub == 0u) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint32_t j = j0 + 4u * i + grp;
+            if (j < nmicro) mst0[j] = m[i];
+        }
+    }
+}
+
 }  // namespace rmq

@@ -49,14 +49,16 @@ inline cudaError_t dev_malloc(void **p, size_t bytes) {
     return cudaMalloc(p, bytes);
 }
 
-// Resident CTAs per SM of `kernel` at `threads` threads (no dynamic shared
-// memory), computed once per cache slot; concurrent first callers compute
-// and store the same value.
+// Resident CTAs per SM of `kernel` at `threads` threads and `dynamic_smem`
+// bytes of dynamic shared memory, computed once per cache slot; concurrent
+// first callers compute and store the same value.
 template <class K>
-cudaError_t occupancy_cached(K kernel, int threads, std::atomic<int> &cache, int &per_sm) {
+cudaError_t occupancy_cached(K kernel, int threads, std::atomic<int> &cache, int &per_sm,
+                             size_t dynamic_smem = 0) {
     int v = cache.load(std::memory_order_relaxed);
     if (v == 0) {
-        const cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0);
+        const cudaError_t err =
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, dynamic_smem);
         if (err != cudaSuccess) return err;
         cache.store(v, std::memory_order_relaxed);
     }
@@ -68,6 +70,7 @@ cudaError_t occupancy_cached(K kernel, int threads, std::atomic<int> &cache, int
 unsigned long long violations_build();
 unsigned long long violations_query();
 unsigned long long violations_batch();
+unsigned long long violations_batch_light();
 unsigned long long violations_persist();
 
 // ---- plain index (build.cu) ----

@@ -713,10 +713,12 @@ __device__ __forceinline__ void flush_stats(const QStats &s, unsigned long long 
 
 // Answer queries [q0, q1) of one array with the whole CTA (THREADS
 // threads) in the queued form, QPT queries per thread per step; `mq` is the
-// calling warp's queue, empty on entry and on return.
-template <bool ALIGNED, bool MICRO, uint32_t MODE, int THREADS, int QPT>
+// calling warp's queue, empty on entry and on return. LIGHT: a light index,
+// `lines` the CTA's line slots (kLineChunks chunks per thread).
+template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, int THREADS, int QPT>
 __device__ __forceinline__ void answer_range_queued(const V1View &v, const QueryOut &o,
-                                                    int64_t q0, int64_t q1, MissQueue &mq) {
+                                                    int64_t q0, int64_t q1, MissQueue &mq,
+                                                    uint4 *lines) {
     constexpr int64_t step = static_cast<int64_t>(THREADS) * QPT;
     QStats s;
     uint32_t waiting = 0;
@@ -724,13 +726,15 @@ __device__ __forceinline__ void answer_range_queued(const V1View &v, const Query
         int2 qq[QPT];
         load_queries<QPT>(o, base, q1, qq);
         if (base + step <= q1)
-            answer_step_queued<ALIGNED, MICRO, false, MODE, THREADS, QPT, false, true>(
-                v, o, base, static_cast<uint32_t>(step), qq, s, mq, waiting);
+            answer_step_queued<ALIGNED, MICRO, LIGHT, MODE, THREADS, QPT, false, true>(
+                v, o, base, static_cast<uint32_t>(step), qq, s, mq, waiting, lines);
         else
-            answer_step_queued<ALIGNED, MICRO, false, MODE, THREADS, QPT, false, false>(
-                v, o, base, static_cast<uint32_t>(q1 - base), qq, s, mq, waiting);
+            answer_step_queued<ALIGNED, MICRO, LIGHT, MODE, THREADS, QPT, false, false>(
+                v, o, base, static_cast<uint32_t>(q1 - base), qq, s, mq, waiting, lines);
     }
-    if (waiting) drain_misses<ALIGNED, MICRO, false, MODE, false>(v, o, mq, waiting, l2_keep_policy(), s, nullptr);
+    if (waiting)
+        drain_misses<ALIGNED, MICRO, LIGHT, MODE, false>(v, o, mq, waiting, l2_keep_policy(), s,
+                                                         lines);
 }
 
 }  // namespace rmq

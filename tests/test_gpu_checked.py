@@ -176,6 +176,23 @@ for seed in range(24):
         v, i = b.run(torch.from_numpy(V).to(dev), torch.from_numpy(Qr).to(dev))
         eq(i.cpu().numpy()[own], ei[own], f"random batch {seed}")
     ran += 1
+    # the same batch as a light plan (block sizes made multiples of 32, >= 64),
+    # and as int32 range maximum over the same values scaled to integers
+    lbs = [0 if x <= 0 else max(64, x // 32 * 32) for x in bucket_bs]
+    with RMQBatch(starts, lengths, qstarts, qcounts, lbs, light=True) as b:
+        dVr, dQr = torch.from_numpy(V).to(dev), torch.from_numpy(Qr).to(dev)
+        v, i = b.run(dVr, dQr)
+        eq(i.cpu().numpy()[own], ei[own], f"random light batch {seed}")
+        v, i = b.run_per_array(dVr, dQr)
+        eq(i.cpu().numpy()[own], ei[own], f"random light batch {seed} per array")
+    Vi = np.round(V * 1000).astype(np.int32)
+    _, eim = TB.expected(oracle, starts[live], lengths[live], qstarts[live], qcounts[live],
+                         -Vi.astype(np.float32), Qr)
+    with RMQBatch(starts, lengths, qstarts, qcounts, lbs, op="max", dtype="int32",
+                  light=bool(seed % 2)) as b:
+        v, i = b.run(torch.from_numpy(Vi).to(dev), torch.from_numpy(Qr).to(dev))
+        eq(i.cpu().numpy()[own], eim[own], f"random int32 max batch {seed}")
+    ran += 2
 
 cnt = C.c_int64()
 rc = L.rmq_checked_violations(C.byref(cnt))

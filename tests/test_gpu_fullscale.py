@@ -106,13 +106,14 @@ def test_tie_heavy_n2e27_q2e26(cuda, native, oracle_lib, length):
     torch.cuda.empty_cache()
 
 
-@pytest.mark.parametrize("bucket_bs", [None, [256] * 32, [64] * 17 + [256] * 15])
-def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs):
+@pytest.mark.parametrize("bucket_bs,light", [(None, False), ([256] * 32, False),
+                                             ([64] * 17 + [256] * 15, False), (None, True)])
+def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs, light):
     """Batched ragged configuration at full size (4096 arrays, lengths
-    round(2^U) with U ~ U[8,22], 2^26 queries): every answer's properties,
-    every answer exactly against HRMQ and a sample against BASE, both on the
-    shared value buffer (a query (l, r) of the array at offset o is the
-    global query (o+l, o+r))."""
+    round(2^U) with U ~ U[8,22], 2^26 queries), full and light index: every
+    answer's properties, every answer exactly against HRMQ and a sample
+    against BASE, both on the shared value buffer (a query (l, r) of the
+    array at offset o is the global query (o+l, o+r))."""
     import torch
 
     from rtxrmq_gb300 import workloads as W
@@ -120,7 +121,7 @@ def test_batched_ragged_full(cuda, native, oracle_lib, bucket_bs):
     w = W.ragged()
     dV = torch.from_numpy(w.values).to(cuda)
     dQ = torch.from_numpy(w.queries).to(cuda)
-    with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, bucket_bs) as b:
+    with RMQBatch(w.starts, w.lengths, w.qstarts, w.qcounts, bucket_bs, light=light) as b:
         v, i = b.run(dV, dQ)
         torch.cuda.synchronize()
         assert b.invalid_count() == 0
