@@ -347,26 +347,29 @@ int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t 
         ws_entries = (ws_entries + 31) & ~int64_t(31);  // 256-byte alignment per array
         b->limit = std::max(b->limit, s + n);
         b->total_q = std::max(b->total_q, qs + qc);
-        if (light) {
-            // A: chunks of micro-blocks; B: block minima at step 1, block
-            // level k at step k + 1; the micro table's levels as tiles at
-            // step 1 (all levels from one read), or level k at step k when
-            // the tiles' halo would not fit
-            for (uint32_t c = 0; c * kLightChunk < a.nmicro; ++c) build.push_back(make_uint2(i, c));
-            if (a.nb > 0) {
-                const uint32_t pb = a.bs / kMicro;
+        if (light && a.nmicro > 0) {
+            // A: tiles (micro-block minima, every micro-table level and, when
+            // the blocks' micro-blocks divide a tile, the block minima, from
+            // one read of the values) if the micro table's halo fits a
+            // tile, else chunks of micro-block minima followed by one table
+            // item per micro level. B: block minima from the micro-block
+            // minima unless the tiles wrote them, then block level k.
+            const uint32_t pb = a.bs / kMicro;
+            if ((1u << (a.mlevels - 1)) - 1u <= kMicroHaloMax) {
+                a.light_flags = kLightTiled | (kMicroTile % pb == 0 ? kLightTileBmin : 0u);
+                for (uint32_t t = 0; t * kMicroTile < a.nmicro; ++t) build.push_back(make_uint2(i, t));
+            } else {
+                for (uint32_t c = 0; c * kLightChunk < a.nmicro; ++c) build.push_back(make_uint2(i, c));
+                for (uint32_t k = 1; k < a.mlevels && (1u << k) <= a.nmicro; ++k)
+                    add_items(k, i, kItemMicroLevel, k, a.nmicro - (1u << k) + 1, lchunk);
+            }
+            const int bstep = (a.light_flags & kLightTileBmin) ? 0 : 1;  // step of block level 0
+            if (bstep == 1)
                 add_items(1, i, kItemBlockMinima, 0, a.nb, std::max<uint32_t>(1u, lchunk / pb));
-            }
             for (uint32_t k = 1; k < a.levels; ++k)
-                add_items(k + 1, i, kItemBlockLevel, k, a.nb - (1u << k) + 1, lchunk);
-            if (a.mlevels >= 2 && a.nmicro >= 2) {
-                if ((1u << (a.mlevels - 1)) - 1u <= kMicroHaloMax)
-                    add_items(1, i, kItemMicroTile, 0, a.nmicro, kMicroTile);
-                else
-                    for (uint32_t k = 1; k < a.mlevels && (1u << k) <= a.nmicro; ++k)
-                        add_items(k, i, kItemMicroLevel, k, a.nmicro - (1u << k) + 1, lchunk);
-            }
-        } else {
+                add_items(static_cast<int>(k) + bstep, i, kItemBlockLevel, k, a.nb - (1u << k) + 1,
+                          lchunk);
+        } else if (!light) {
             const uint32_t nunits = unit_count(a.nb, a.U);
             for (uint32_t u = 0; u < nunits; ++u) build.push_back(make_uint2(i, u));
             for (uint32_t k = 1; k < a.levels; ++k)

@@ -28,6 +28,9 @@
 #ifndef RMQ_BATCH_MINB
 #define RMQ_BATCH_MINB 4
 #endif
+#ifndef RMQ_BATCH_LIGHT_MINB
+#define RMQ_BATCH_LIGHT_MINB 3  // the light-index kernels
+#endif
 
 namespace rmq {
 
@@ -47,13 +50,18 @@ enum : uint32_t {
     kItemBlockLevel = 0,   // block-table level k from level k - 1
     kItemBlockMinima = 1,  // block-table level 0 from the micro-block minima
     kItemMicroLevel = 2,   // micro-table level k from level k - 1
-    kItemMicroTile = 3,    // every micro-table level of a tile, in shared memory
 };
-// Micro-table tiles: kMicroTile offsets per level from one read of the tile's
-// minima plus a halo of 2^(mlevels - 1) - 1 (at most kMicroHaloMax, blocks up
-// to 65536 elements; larger blocks take one item per level).
+// Light tiles (phase A items of a light array whose micro table is shallow
+// enough): kMicroTile micro-blocks whose minima, every micro-table level and
+// the minima of the blocks inside come from one read of the tile's values
+// plus a halo of 2^(mlevels - 1) - 1 micro-blocks (at most kMicroHaloMax:
+// blocks up to 65536 elements). Other light arrays take chunks in phase A
+// and one table item per level.
 constexpr uint32_t kMicroTile = 2048;
 constexpr uint32_t kMicroHaloMax = 2047;
+// BatchArray::light_flags
+constexpr uint32_t kLightTiled = 1;       // phase A items are tiles
+constexpr uint32_t kLightTileBmin = 2;    // tiles also write the block minima (bs / 32 divides kMicroTile)
 
 struct BatchArray {
     int64_t off;    // first value in the buffer
@@ -63,7 +71,7 @@ struct BatchArray {
     int64_t mst;    // workspace entry offset of the micro-block minima (light)
     int64_t moff;   // workspace entry offset of the micro-table offsets (light)
     uint32_t n, bs, nb, levels;
-    uint32_t nmicro, mlevels, moff_bytes, pad;
+    uint32_t nmicro, mlevels, moff_bytes, light_flags;
     UnitLayout U;
     Div31 dv;
 };
@@ -95,7 +103,7 @@ constexpr size_t kLightSmemBytes =
     kLightQueueBytes + sizeof(uint4) * kLineChunks * static_cast<size_t>(kBatchThreads);
 static_assert(kLightQueueBytes % 16 == 0, "line slots start 16-byte aligned");
 static_assert((kMicroTile + kMicroHaloMax) * (sizeof(Entry) + sizeof(uint16_t)) <= kLightSmemBytes,
-              "a micro-table tile fits the light CTA's shared memory");
+              "a light tile fits the light CTA's shared memory");
 
 // Light kernels (batch_light.cu): the instantiation for (aligned, key mode),
 // its dynamic shared memory and CTAs per SM (the dynamic-memory limit set).
@@ -174,9 +182,9 @@ __device__ __forceinline__ void light_chunk(const BatchParams &P, const BatchArr
     Entry m[4];
     // whole rows inside the array, 16-byte aligned
     if (ALIGNED && a.off % 4 == 0 && (j0 + kMicroPerWarp) * kMicroElems <= a.n)
-        micro_min_warp<MODE, true>(A, a.n, a.nmicro, j0, P.ws + a.mst, m);
+        micro_min_warp<MODE, true>(A, a.n, j0, a.nmicro, P.ws + a.mst, 0u, m);
     else
-        micro_min_warp<MODE, false>(A, a.n, a.nmicro, j0, P.ws + a.mst, m);
+        micro_min_warp<MODE, false>(A, a.n, j0, a.nmicro, P.ws + a.mst, 0u, m);
 }
 
 // Light table step, kind kItemBlockMinima: block minima of blocks [first,
@@ -217,29 +225,18 @@ __device__ __forceinline__ void light_micro_level_w(const BatchParams &P, const 
         micro_level_at(P.ws + a.mst, cur, prev, a.nmicro, k, i);
 }
 
-// Light table step, kind kItemMicroTile: every level 1 .. mlevels - 1 of the
-// micro table at positions [t0, t0 + count) (count <= kMicroTile) from one
-// read of the minima of [t0, t0 + count + halo) into shared memory. Each
-// level keeps, per position, the tile-local index of its window's best
-// micro-block (the level below's two halves compared); positions whose
-// window leaves the loaded range are dropped level by level. Two barriers
-// per level separate the reads of the level below from the overwrite.
+// Every level 1 .. mlevels - 1 of the micro table at positions [t0, t0 +
+// count) from the minima key[0 .. e) of micro-blocks [t0, t0 + e) in shared
+// memory (best[i] = i on entry). Each level keeps, per position, the
+// tile-local index of its window's best micro-block (the level below's two
+// halves compared); positions whose window leaves the loaded range are
+// dropped level by level. Two barriers per level separate the reads of the
+// level below from the overwrite.
 template <class O>
-__device__ __forceinline__ void light_micro_tile(const BatchParams &P, const BatchArray &a,
-                                                 uint32_t t0, uint32_t count,
-                                                 unsigned char *smem) {
-    constexpr uint32_t kMaxE = kMicroTile + kMicroHaloMax;
-    constexpr int kPer = (kMaxE + kBatchThreads - 1) / kBatchThreads;
-    Entry *key = reinterpret_cast<Entry *>(smem);
-    uint16_t *best = reinterpret_cast<uint16_t *>(key + kMaxE);
-    const uint32_t halo = (1u << (a.mlevels - 1)) - 1u;
-    const uint32_t e = min(t0 + count + halo, a.nmicro) - t0;  // entries loaded
-    const Entry *mst = P.ws + a.mst;
-    for (uint32_t i = threadIdx.x; i < e; i += kBatchThreads) {
-        key[i] = rmq_chk(i < kMaxE) ? mst[t0 + i] : kEntryNone;
-        best[i] = static_cast<uint16_t>(i);
-    }
-    __syncthreads();
+__device__ __forceinline__ void micro_tile_levels(const BatchParams &P, const BatchArray &a,
+                                                  uint32_t t0, uint32_t count, uint32_t e,
+                                                  const Entry *key, uint16_t *best) {
+    constexpr int kPer = (kMicroTile + kMicroHaloMax + kBatchThreads - 1) / kBatchThreads;
     O *off = reinterpret_cast<O *>(P.ws + a.moff);
     for (uint32_t k = 1; k < a.mlevels && (1u << k) <= e; ++k) {
         const uint32_t half = 1u << (k - 1);
@@ -268,11 +265,71 @@ __device__ __forceinline__ void light_micro_tile(const BatchParams &P, const Bat
     }
 }
 
-// Phase B: table steps 1 .. maxlev - 1, a grid barrier after each. `smem`:
-// the light CTA's shared memory (micro-table tiles), null otherwise.
+// Light phase A, one tile (kLightTiled arrays): the minima of micro-blocks
+// [t0, t0 + count + halo) from the values into shared memory (16 per warp
+// per step, as light_chunk), the tile's own minima to the micro-block minima
+// table, the minima of the blocks inside the tile (kLightTileBmin), and every
+// micro-table level at [t0, t0 + count). The halo's minima are computed
+// again by the next tile.
+template <bool ALIGNED, uint32_t MODE, class O>
+__device__ __forceinline__ void light_tile(const BatchParams &P, const BatchArray &a, uint32_t t,
+                                           unsigned char *smem) {
+    constexpr uint32_t kMaxE = kMicroTile + kMicroHaloMax;
+    Entry *key = reinterpret_cast<Entry *>(smem);
+    uint16_t *best = reinterpret_cast<uint16_t *>(key + kMaxE);
+    const uint32_t t0 = t * kMicroTile;
+    const uint32_t count = min(kMicroTile, a.nmicro - t0);
+    const uint32_t halo = (1u << (a.mlevels - 1)) - 1u;
+    const uint32_t jend = min(t0 + count + halo, a.nmicro);
+    const uint32_t e = jend - t0;  // minima held in shared memory
+    const float *A = P.A + a.off;
+    const bool vec = ALIGNED && a.off % 4 == 0;
+    // 8 rows (32 micro-blocks, 4 KB) per warp step: 96 KB of loads in flight per SM
+    constexpr uint32_t kRows = 8, kPerWarp = 4 * kRows;
+    for (uint32_t j0 = t0 + (threadIdx.x >> 5) * kPerWarp; j0 < jend;
+         j0 += kPerWarp * (kBatchThreads / 32)) {
+        if (vec && (j0 + kPerWarp) * kMicroElems <= a.n)
+            micro_min_rows<MODE, true, kRows>(A, a.n, j0, jend, key, t0);
+        else
+            micro_min_rows<MODE, false, kRows>(A, a.n, j0, jend, key, t0);
+    }
+    __syncthreads();
+    Entry *mst = P.ws + a.mst;
+    for (uint32_t i = threadIdx.x; i < e; i += kBatchThreads) {
+        if (i < count) mst[t0 + i] = key[i];
+        best[i] = static_cast<uint16_t>(i);
+    }
+    if (a.light_flags & kLightTileBmin) {
+        // blocks [t0 / pb, (t0 + count - 1) / pb], all inside the tile
+        const uint32_t pb = a.bs / kMicroElems;
+        const uint32_t b0 = t0 / pb, nbt = (count + pb - 1) / pb;
+        Entry *bmin = P.ws + a.st;
+        if (pb <= 16u) {
+            for (uint32_t x = threadIdx.x; x < nbt; x += kBatchThreads) {
+                Entry mm = kEntryNone;
+                const uint32_t j1 = min(x * pb + pb, count);
+                for (uint32_t j = x * pb; j < j1; ++j) mm = better(mm, key[j]);
+                if (rmq_chk(b0 + x < a.nb)) bmin[b0 + x] = mm;
+            }
+        } else {
+            const uint32_t lane = threadIdx.x & 31u;
+            for (uint32_t x = threadIdx.x >> 5; x < nbt; x += kBatchThreads / 32) {
+                Entry mm = kEntryNone;
+                const uint32_t j1 = min(x * pb + pb, count);
+                for (uint32_t j = x * pb + lane; j < j1; j += 32u) mm = better(mm, key[j]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mm = better(mm, __shfl_xor_sync(0xffffffffu, mm, o));
+                if (lane == 0u && rmq_chk(b0 + x < a.nb)) bmin[b0 + x] = mm;
+            }
+        }
+    }
+    __syncthreads();
+    micro_tile_levels<O>(P, a, t0, count, e, key, best);
+}
+
+// Phase B: table steps 1 .. maxlev - 1, a grid barrier after each.
 template <bool LIGHT>
-__device__ __forceinline__ void table_steps(const BatchParams &P, cg::grid_group &grid,
-                                            unsigned char *smem) {
+__device__ __forceinline__ void table_steps(const BatchParams &P, cg::grid_group &grid) {
     for (int s = 1; (P.phases & 2u) && s < P.maxlev; ++s) {
         for (int32_t it = P.lvl_start[s] + blockIdx.x; it < P.lvl_start[s + 1]; it += gridDim.x) {
             const uint4 w = P.lvl[it];
@@ -280,11 +337,6 @@ __device__ __forceinline__ void table_steps(const BatchParams &P, cg::grid_group
             const uint32_t kind = w.y >> 16, k = w.y & 0xffffu;
             if (LIGHT && kind == kItemBlockMinima) {
                 light_block_minima(P, a, w.z, w.w);
-            } else if (LIGHT && kind == kItemMicroTile) {
-                if (a.moff_bytes == 1u)
-                    light_micro_tile<uint8_t>(P, a, w.z, w.w, smem);
-                else
-                    light_micro_tile<uint16_t>(P, a, w.z, w.w, smem);
             } else if (LIGHT && kind == kItemMicroLevel) {
                 if (a.moff_bytes == 1u)
                     light_micro_level_w<uint8_t>(P, a, k, w.z, w.w);
@@ -337,7 +389,7 @@ __global__ void __launch_bounds__(kBatchThreads, RMQ_BATCH_MINB) batch_kernel(Ba
         build_unit<ALIGNED, MODE>(unit_job<MODE>(P, w.x), w.y, stage, s_warp, s_flag);
     }
     grid.sync();
-    table_steps<false>(P, grid, nullptr);
+    table_steps<false>(P, grid);
     // C: the warps' miss queues live in the staging memory of phase A
     static_assert(sizeof(MissQueue) * (kBatchThreads / 32) <= sizeof(Entry) * kStageEntries,
                   "miss queues fit the staging memory");
@@ -348,17 +400,25 @@ __global__ void __launch_bounds__(kBatchThreads, RMQ_BATCH_MINB) batch_kernel(Ba
 // Light index: block and micro-block tables only. Dynamic shared memory
 // (kLightSmemBytes): miss queues, then the threads' line slots.
 template <bool ALIGNED, uint32_t MODE>
-__global__ void __launch_bounds__(kBatchThreads, RMQ_BATCH_MINB) batch_kernel_light(BatchParams P) {
+__global__ void __launch_bounds__(kBatchThreads, RMQ_BATCH_LIGHT_MINB)
+batch_kernel_light(BatchParams P) {
     extern __shared__ __align__(16) unsigned char s_light[];
     cg::grid_group grid = cg::this_grid();
 
-    // A: micro-block minima
+    // A: tiles (micro-block minima, micro table, block minima) or chunks
+    // (micro-block minima only)
     for (int32_t it = (P.phases & 1u) ? blockIdx.x : P.nbuild; it < P.nbuild; it += gridDim.x) {
         const uint2 w = P.build[it];
-        light_chunk<ALIGNED, MODE>(P, P.arrays[w.x], w.y);
+        const BatchArray &a = P.arrays[w.x];
+        if (!(a.light_flags & kLightTiled))
+            light_chunk<ALIGNED, MODE>(P, a, w.y);
+        else if (a.moff_bytes == 1u)
+            light_tile<ALIGNED, MODE, uint8_t>(P, a, w.y, s_light);
+        else
+            light_tile<ALIGNED, MODE, uint16_t>(P, a, w.y, s_light);
     }
     grid.sync();
-    table_steps<true>(P, grid, s_light);
+    table_steps<true>(P, grid);
     MissQueue &mq = reinterpret_cast<MissQueue *>(s_light)[threadIdx.x >> 5];
     uint4 *lines = reinterpret_cast<uint4 *>(s_light + kLightQueueBytes);
     query_items<ALIGNED, true, MODE>(P, mq, lines);

@@ -159,9 +159,9 @@ micro_min_kernel(const float *__restrict__ A, uint32_t n, uint32_t nmicro, uint3
         const uint32_t j0 = w * kMicroPerWarp;
         Entry m[4];  // micro-block j0 + 4i + grp, on all 8 lanes of the group
         if (aligned && (j0 + kMicroPerWarp) * kMicro <= n)
-            micro_min_warp<MODE, true>(A, n, nmicro, j0, mst0, m);
+            micro_min_warp<MODE, true>(A, n, j0, nmicro, mst0, 0u, m);
         else
-            micro_min_warp<MODE, false>(A, n, nmicro, j0, mst0, m);
+            micro_min_warp<MODE, false>(A, n, j0, nmicro, mst0, 0u, m);
         const uint32_t jl = min(j0 + kMicroPerWarp, nmicro) - 1u;
         if (j0 / per_block == jl / per_block) {
             // one block: micro-blocks past nmicro hold kEntryNone, the identity

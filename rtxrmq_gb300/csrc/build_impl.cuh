@@ -793,16 +793,16 @@ __device__ __forceinline__ void micro_level_at(const Entry *__restrict__ mst0, O
 }
 
 // Micro-block minima of micro-blocks [j0, j0 + 16) of one array (values
-// A[0 .. n), nmicro = ceil(n / 32)) with one whole warp: four 512-byte rows,
-// each lane 4 consecutive elements of every row, all loads in flight before
-// any reduction (micro_row_min). VEC: 16-byte loads (A + j0 * 32 16-byte
-// aligned and all 512 elements inside the array). Writes mst0[j] for j <
-// nmicro; returns the four minima of the lane's group (micro-blocks j0 + 4i
-// + lane / 8; kEntryNone past nmicro).
+// A[0 .. n)) with one whole warp: four 512-byte rows, each lane 4
+// consecutive elements of every row, all loads in flight before any
+// reduction (micro_row_min). VEC: 16-byte loads (A + j0 * 32 16-byte aligned
+// and all 512 elements inside the array). Writes dst[j - base] for j < jend
+// (jend <= ceil(n / 32)); returns the four minima of the lane's group
+// (micro-blocks j0 + 4i + lane / 8; kEntryNone past the array).
 template <uint32_t MODE, bool VEC>
 __device__ __forceinline__ void micro_min_warp(const float *__restrict__ A, uint32_t n,
-                                               uint32_t nmicro, uint32_t j0, Entry *mst0,
-                                               Entry (&m)[4]) {
+                                               uint32_t j0, uint32_t jend, Entry *dst,
+                                               uint32_t base, Entry (&m)[4]) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t sub = lane & 7u;
     const uint32_t grp = lane >> 3;
@@ -832,8 +832,46 @@ __device__ __forceinline__ void micro_min_warp(const float *__restrict__ A, uint
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const uint32_t j = j0 + 4u * i + grp;
-            if (j < nmicro) mst0[j] = m[i];
+            if (j < jend) dst[j - base] = m[i];
         }
+    }
+}
+
+// micro_min_warp over ROWS rows (4 * ROWS micro-blocks [j0, j0 + 4 ROWS)),
+// every row's loads in flight before any reduction, each row's minima
+// written (dst[j - base], j < jend) as soon as they are reduced, none kept.
+template <uint32_t MODE, bool VEC, int ROWS>
+__device__ __forceinline__ void micro_min_rows(const float *__restrict__ A, uint32_t n,
+                                               uint32_t j0, uint32_t jend, Entry *dst,
+                                               uint32_t base) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t sub = lane & 7u;
+    const uint32_t grp = lane >> 3;
+    const uint32_t e0 = j0 * kMicroElems + lane * 4u;
+    uint32_t b[ROWS][4];
+    if (VEC) {
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i) {
+            const uint4 f = ld_u4(A + e0 + i * 128u);
+            b[i][0] = f.x;
+            b[i][1] = f.y;
+            b[i][2] = f.z;
+            b[i][3] = f.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t g = e0 + i * 128u + k;
+                b[i][k] = g < n ? ld_u1(A + g) : 0u;
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i) {
+        const Entry m = micro_row_min<MODE, VEC>(b[i], e0 + i * 128u, n, grp, sub);
+        const uint32_t j = j0 + 4u * i + grp;
+        if (sub == 0u && j < jend) dst[j - base] = m;
     }
 }
 

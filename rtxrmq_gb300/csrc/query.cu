@@ -23,6 +23,9 @@ constexpr int kQPT = RMQ_QUERY_QPT;
 #ifndef RMQ_QUERY_MINB
 #define RMQ_QUERY_MINB 1  // CTAs per SM the query kernel is compiled for (a register bound)
 #endif
+#ifndef RMQ_QUERY_LIGHT_MINB
+#define RMQ_QUERY_LIGHT_MINB 3  // the same for the light-index instantiations (68 registers)
+#endif
 
 // Queries base + t + k * kThreads (k < kQPT) of a full step, no bounds checks.
 __device__ __forceinline__ void load_full(const QueryOut &o, int64_t base, int2 (&qq)[kQPT]) {
@@ -39,7 +42,7 @@ __device__ __forceinline__ void load_full(const QueryOut &o, int64_t base, int2 
 // measurement instantiation (rmq_query_stats), which also counts how each
 // query was settled and what it read into stats[kStatCount].
 template <bool ALIGNED, bool MICRO, bool LIGHT, uint32_t MODE, bool STATS>
-__global__ void __launch_bounds__(kThreads, RMQ_QUERY_MINB)
+__global__ void __launch_bounds__(kThreads, LIGHT ? RMQ_QUERY_LIGHT_MINB : RMQ_QUERY_MINB)
 query_kernel(V1View v, QueryOut o, int64_t q, unsigned long long *stats) {
     __shared__ MissQueue s_mq[kThreads / 32];
     // light index only: each thread's slot for the line copies of its

@@ -389,27 +389,46 @@ __device__ __forceinline__ Entry line_min_async(const V1View &v, uint32_t lo, ui
     const int64_t p0 = glo & ~int64_t(3);
     const int nc = static_cast<int>(((ghi & ~int64_t(3)) - p0) / 4) + 1;
     const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(slot));
-    for (int c = 0; c < nc; ++c) {
-        const int64_t p = p0 + 4 * c;
-        const int64_t avail = v.limit - p;  // elements of the chunk inside the buffer
-        const uint32_t bytes = avail >= 4 ? 16u : static_cast<uint32_t>(avail > 0 ? avail * 4 : 0);
-        if (rmq_chk(p >= 0 && bytes > 0u))
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                         :: "r"(sbase + 16u * c), "l"(v.A + p), "r"(bytes) : "memory");
+    const float *base = v.A + p0;  // 16-byte aligned
+    const int64_t room = v.limit - p0;  // elements from base to the end of the buffer
+    if (room >= 4 * nc) {
+#pragma unroll 1
+        for (int c = 0; c < nc; ++c)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                         :: "r"(sbase + 16u * c), "l"(base + 4 * c) : "memory");
+    } else {
+        // the buffer ends inside the line: copy what lies inside it
+#pragma unroll 1
+        for (int c = 0; c < nc; ++c) {
+            const int64_t avail = room - 4 * c;  // elements of the chunk inside the buffer
+            const uint32_t bytes = avail >= 4 ? 16u : static_cast<uint32_t>(avail > 0 ? avail * 4 : 0);
+            if (rmq_chk(p0 >= 0 && bytes > 0u))
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                             :: "r"(sbase + 16u * c), "l"(base + 4 * c), "r"(bytes) : "memory");
+        }
     }
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-    Entry best = kEntryNone;
+    // 32-bit keys first, one composite at the end: the smallest key and the
+    // first local index holding it (strict <, in index order) is the
+    // leftmost best; if every key is the largest, that is element lo.
+    const int32_t l0 = static_cast<int32_t>(p0 - v.off);  // local index of slot[0].x
+    uint32_t km = 0xffffffffu, pos = lo, nz = 0u;
+#pragma unroll 1
     for (int c = 0; c < nc; ++c) {
         const uint4 f = slot[c];
         const uint32_t w[4] = {f.x, f.y, f.z, f.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const int64_t g = p0 + 4 * c + k;
-            if (g >= glo && g <= ghi)
-                best = better(best, make_entry(w[k], static_cast<uint32_t>(g - v.off), MODE));
+            const int32_t li = l0 + 4 * c + k;
+            const uint32_t kk = key_of(w[k], MODE);
+            if (static_cast<uint32_t>(li - static_cast<int32_t>(lo)) <= hi - lo && kk < km) {
+                km = kk;
+                pos = static_cast<uint32_t>(li);
+                nz = negzero_of(w[k], MODE);
+            }
         }
     }
-    return best;
+    return (static_cast<uint64_t>(km) << 32) | (pos << 1) | nz;
 }
 
 // Leftmost best of local A[lo..hi] inside one micro-block for a miss: the
@@ -421,33 +440,38 @@ __device__ __forceinline__ Entry line_min(const V1View &v, uint32_t lo, uint32_t
     return thread_range_min<ALIGNED>(v, lo, hi, MODE);
 }
 
-// The part of a query in its end unit on the left, [l, end of l's unit]
-// (micro-block, or block a), and on the right, [start of r's unit, r]. With
-// per-element entries one entry each; in a light index (no entries) one
-// line of values inside the end micro-block, plus the micro table over the
-// block's whole micro-blocks for a block part.
-template <bool ALIGNED, bool LIGHT, uint32_t MODE, bool STATS>
-__device__ __forceinline__ Entry left_part(const V1View &v, bool micro, uint32_t a, uint32_t l,
-                                           uint64_t pol, QStats &s, uint4 *slot) {
-    if constexpr (!LIGHT) return left_entry<STATS>(v, micro, l, s);
-    const uint32_t ml = l >> 5;
-    const uint32_t end = min(ml * 32u + 31u, v.n - 1u);
-    const Entry line = line_min<ALIGNED, MODE>(v, l, end, slot);
-    if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, l, end);
-    if (micro) return line;
-    const uint32_t me = (((a + 1u) * v.bs) >> 5) - 1u;  // block a is full: a < b
-    return ml < me ? better(line, micro_probe<STATS>(v, ml + 1u, me, pol, s)) : line;
+// With per-element entries, the part of a query in its end unit on the
+// left, [l, end of l's unit] (micro-block, or block), and on the right,
+// [start of r's unit, r]: one entry each.
+template <bool STATS>
+__device__ __forceinline__ Entry left_part(const V1View &v, bool micro, uint32_t l, QStats &s) {
+    return left_entry<STATS>(v, micro, l, s);
 }
-template <bool ALIGNED, bool LIGHT, uint32_t MODE, bool STATS>
-__device__ __forceinline__ Entry right_part(const V1View &v, bool micro, uint32_t b, uint32_t r,
-                                            uint64_t pol, QStats &s, uint4 *slot) {
-    if constexpr (!LIGHT) return right_entry<STATS>(v, micro, r, s);
-    const uint32_t mr = r >> 5;
-    const Entry line = line_min<ALIGNED, MODE>(v, mr * 32u, r, slot);
-    if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, mr * 32u, r);
+template <bool STATS>
+__device__ __forceinline__ Entry right_part(const V1View &v, bool micro, uint32_t r, QStats &s) {
+    return right_entry<STATS>(v, micro, r, s);
+}
+
+// Light index: the query's part in its end unit on one side, [l, end of
+// l's unit] (left) or [start of r's unit, r] (right): one line of values
+// inside the end micro-block, plus for a block unit the micro table over
+// the block's whole micro-blocks on that side. The side is a value, not a
+// branch, so lanes settling left and right parts run the same code.
+template <bool ALIGNED, uint32_t MODE, bool STATS>
+__device__ __forceinline__ Entry light_part(const V1View &v, bool micro, bool left, uint32_t a,
+                                            uint32_t b, uint32_t l, uint32_t r, uint64_t pol,
+                                            QStats &s, uint4 *slot) {
+    const uint32_t lo = left ? l : (r & ~31u);
+    const uint32_t hi = left ? min(l | 31u, v.n - 1u) : r;
+    const Entry line = line_min<ALIGNED, MODE>(v, lo, hi, slot);
+    if constexpr (STATS) s.c[kStatSectors] += range_sectors(v, lo, hi);
     if (micro) return line;
-    const uint32_t ms = (b * v.bs) >> 5;
-    return ms < mr ? better(micro_probe<STATS>(v, ms, mr - 1u, pol, s), line) : line;
+    // block a is full when a < b: its last micro-block ends inside the array
+    const uint32_t ml = l >> 5, me = (((a + 1u) * v.bs) >> 5) - 1u;
+    const uint32_t mr = r >> 5, ms = (b * v.bs) >> 5;
+    const bool has = left ? ml < me : ms < mr;
+    if (!has) return line;
+    return better(line, micro_probe<STATS>(v, left ? ml + 1u : ms, left ? me : mr - 1u, pol, s));
 }
 
 // Settles one query whose superset best lay outside [l, r] (or, without
@@ -459,33 +483,58 @@ __device__ __forceinline__ Entry finish_miss(const V1View &v, uint32_t l, uint32
                                              uint32_t code, uint64_t pol, QStats &s,
                                              uint4 *slot) {
     const uint32_t path = code & 7u;
-    if (path == kPathBlock) {
-        if constexpr (STATS) s.c[kStatBlockEdge] += 1u;
-        const uint32_t bstart = div31(l, v.dv) * v.bs;
-        const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
-        return r == bend ? left_entry<STATS>(v, false, l, s) : right_entry<STATS>(v, false, r, s);
+    if constexpr (LIGHT) {
+        // one copy of the part's code: the second pass (the other end, after
+        // the middle units) runs only for the rare query the narrower probe
+        // does not settle
+        const bool micro = path == kPathMicroTable;
+        const uint32_t a = micro ? (l >> 5) : div31(l, v.dv);
+        const uint32_t b = micro ? (r >> 5) : div31(r, v.dv);
+        bool left = (code & kMissLeft) != 0u;
+        const Entry e2 = unit_probe<STATS>(v, micro, left ? a + 1u : a, left ? b : b - 1u, pol, s);
+        Entry res = kEntryNone;
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            res = better(res, light_part<ALIGNED, MODE, STATS>(v, micro, left, a, b, l, r, pol, s,
+                                                               slot));
+            if (pass == 1) break;
+            const uint32_t m2 = entry_idx(e2);
+            if (left ? m2 <= r : m2 >= l) {
+                if constexpr (STATS) s.c[kStatSecond] += 1u;
+                return better(res, e2);
+            }
+            if constexpr (STATS) s.c[kStatFull] += 1u;
+            if (b - a >= 2u) res = better(res, unit_probe<STATS>(v, micro, a + 1u, b - 1u, pol, s));
+            left = !left;
+        }
+        return res;
+    } else {
+        if (path == kPathBlock) {
+            if constexpr (STATS) s.c[kStatBlockEdge] += 1u;
+            const uint32_t bstart = div31(l, v.dv) * v.bs;
+            const uint32_t bend = min(bstart + v.bs, v.n) - 1u;
+            return r == bend ? left_entry<STATS>(v, false, l, s) : right_entry<STATS>(v, false, r, s);
+        }
+        const bool micro = path == kPathMicroTable;
+        const uint32_t a = micro ? (l >> 5) : div31(l, v.dv);
+        const uint32_t b = micro ? (r >> 5) : div31(r, v.dv);
+        const bool left = (code & kMissLeft) != 0u;
+        // the narrower probe first: its loads are in flight while the part's
+        // entry is loaded
+        const Entry e2 = left ? unit_probe<STATS>(v, micro, a + 1u, b, pol, s)
+                              : unit_probe<STATS>(v, micro, a, b - 1u, pol, s);
+        const Entry e1 = left ? left_part<STATS>(v, micro, l, s) : right_part<STATS>(v, micro, r, s);
+        const uint32_t m2 = entry_idx(e2);
+        if (left ? m2 <= r : m2 >= l) {
+            if constexpr (STATS) s.c[kStatSecond] += 1u;
+            return better(e1, e2);
+        }
+        if constexpr (STATS) s.c[kStatFull] += 1u;
+        const Entry mid = (b - a >= 2u) ? unit_probe<STATS>(v, micro, a + 1u, b - 1u, pol, s)
+                                        : kEntryNone;
+        const Entry other = left ? right_part<STATS>(v, micro, r, s) : left_part<STATS>(v, micro, l, s);
+        return better(better(e1, other), mid);
     }
-    const bool micro = path == kPathMicroTable;
-    const uint32_t a = micro ? (l >> 5) : div31(l, v.dv);
-    const uint32_t b = micro ? (r >> 5) : div31(r, v.dv);
-    const bool left = (code & kMissLeft) != 0u;
-    // the narrower probe first: its loads are in flight while the part's
-    // line is copied
-    const Entry e2 = left ? unit_probe<STATS>(v, micro, a + 1u, b, pol, s)
-                          : unit_probe<STATS>(v, micro, a, b - 1u, pol, s);
-    const Entry e1 = left ? left_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, a, l, pol, s, slot)
-                          : right_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, b, r, pol, s, slot);
-    const uint32_t m2 = entry_idx(e2);
-    if (left ? m2 <= r : m2 >= l) {
-        if constexpr (STATS) s.c[kStatSecond] += 1u;
-        return better(e1, e2);
-    }
-    if constexpr (STATS) s.c[kStatFull] += 1u;
-    const Entry mid = (b - a >= 2u) ? unit_probe<STATS>(v, micro, a + 1u, b - 1u, pol, s)
-                                    : kEntryNone;
-    const Entry other = left ? right_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, b, r, pol, s, slot)
-                             : left_part<ALIGNED, LIGHT, MODE, STATS>(v, micro, a, l, pol, s, slot);
-    return better(better(e1, other), mid);
 }
 
 // One warp's queue: up to 31 waiting queries plus the 32 that one query
