@@ -415,6 +415,23 @@ def sweep_block_sizes(R, dA, dQ, out_v, out_i, bs_list, stream, barrier, q, worl
     return sweep
 
 
+def timed_build(make, reps: int = 5):
+    """(index, median wall-clock ms of `reps` constructions including the
+    allocation, as the reference's `construction` column counts it); all but
+    the last index are freed."""
+    import torch
+    times, ix = [], None
+    for r in range(reps):
+        if ix is not None:
+            ix.close()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ix = make()
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t) * 1e3)
+    return ix, statistics.median(times)
+
+
 def pick(sweep, lo, hi):
     cand = [(k, v) for k, v in sweep.items() if lo <= k <= hi]
     return max(cand, key=lambda kv: kv[1]) if cand else None
@@ -435,11 +452,7 @@ def bench_plain_mode(R, dA, n, Q, out_v, out_i, args, stream, barrier, world, de
         sweep = sweep_block_sizes(R, dA, dQ, out_v, out_i, BS_BELOW + BS_RANGE, stream, barrier,
                                   q, world)
         bs = pick(sweep, BS_RANGE[0], BS_RANGE[-1])[0]
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    ix = R.RMQIndex(dA, bs)
-    torch.cuda.synchronize()
-    construction_ms = (time.perf_counter() - t) * 1e3
+    ix, construction_ms = timed_build(lambda: R.RMQIndex(dA, bs))
     fn = lambda: ix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
     ms = time_steps(fn, args.steps, args.warmup, stream, barrier)
     st = ix.query_stats(dQ)
@@ -454,11 +467,7 @@ def bench_plain_mode(R, dA, n, Q, out_v, out_i, args, stream, barrier, world, de
     # the light index (RMQ_BUILD_LIGHT) at the same block size: tables only,
     # its construction, size and query time beside the full index's
     if bs % 32 == 0 and bs >= 64:
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        lix = R.RMQIndex(dA, bs, light=True)
-        torch.cuda.synchronize()
-        lc_ms = (time.perf_counter() - t) * 1e3
+        lix, lc_ms = timed_build(lambda: R.RMQIndex(dA, bs, light=True))
         lfn = lambda: lix.query(dQ, out_val=out_v, out_idx=out_i)  # noqa: E731
         lms = time_steps(lfn, args.steps, args.warmup, stream, barrier)
         res["light_index"] = {"rmq_s": job_rate(q, world, lms), "ms_per_step": lms,

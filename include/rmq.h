@@ -427,7 +427,9 @@ int rmq_batch_autotune(int32_t narrays, const int64_t *h_starts,
 
 /*
  * rmq_batch_autotune over the whole tile: per bucket present, first the
- * block size (as rmq_batch_autotune), then with it the query-item size
+ * block size (as rmq_batch_autotune; for a light plan 4096, 1024 or 16384,
+ * another than 4096 only when it is more than 3% faster), then with it the
+ * query-item size
  * (512 .. 8192 queries) and then the level-item size (1024 .. 16384
  * entries), each the fastest over `reps` runs of a plan holding only that
  * bucket's arrays, built with `flags` (as rmq_batch_create_ex); absent

@@ -159,6 +159,11 @@ int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_
         if (h_lengths[i] > 0) members[bucket_of(h_lengths[i])].push_back(i);  // empty: no structure
     }
     static const int32_t bs_cands[] = {64, 256, 1024, 4096, 16384, 65536};
+    // light plans: small blocks send short queries through the coarser block
+    // probe, so only these, starting from the default; another is taken only
+    // when it is more than 3% faster (per-bucket timings are short and noisy)
+    static const int32_t light_cands[] = {4096, 1024, 16384};
+    const bool light = (flags & RMQ_BUILD_LIGHT) != 0;
     static const int32_t q_cands[] = {512, 1024, 2048, 4096, 8192};
     static const int32_t l_cands[] = {1024, 4096, 16384};
     cudaEvent_t e0, e1;
@@ -180,14 +185,18 @@ int autotune_buckets(int32_t narrays, const int64_t *h_starts, const int64_t *h_
         const int64_t maxlen = int64_t(2) << bk;
         rmq_batch_tile_t best{0, static_cast<int32_t>(kQueryChunk), static_cast<int32_t>(kLevelChunk), 0};
         float best_ms = 0.f;
-        for (int32_t c : bs_cands) {
-            if (c > 2 * maxlen && best.bs != 0) break;
+        const int32_t *cands = light ? light_cands : bs_cands;
+        const int ncand = light ? 3 : 6;
+        for (int ci = 0; ci < ncand; ++ci) {
+            const int32_t c = cands[ci];
+            if (!light && c > 2 * maxlen && best.bs != 0) break;
+            if (light && c > 2 * maxlen && c > cands[0]) continue;
             rmq_batch_tile_t t = best;
             t.bs = c;
             const float ms = time_bucket(s, l, qs, qc, bk, t, flags, d_vals, d_queries, d_val,
                                          d_idx, reps, stream, e0, e1, rc);
             if (rc) break;
-            if (best.bs == 0 || ms < best_ms) {
+            if (best.bs == 0 || ms < (light ? 0.97f : 1.f) * best_ms) {
                 best_ms = ms;
                 best = t;
             }
