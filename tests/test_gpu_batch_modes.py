@@ -34,11 +34,15 @@ def run_all(cuda, b, A, Q):
 
 
 @pytest.mark.parametrize("seed,ties,align", [(1, False, 1), (2, True, 1), (3, False, 4), (4, True, 4)])
-@pytest.mark.parametrize("cfg", ["default", "small", "large", "mixed"])
+@pytest.mark.parametrize("cfg", ["default", "small", "large", "huge", "mixed"])
 def test_batch_light_matches_oracle(cuda, native, oracle_lib, seed, ties, align, cfg):
+    """Light plans at every block-size class: tiles with block minima (bs/32
+    dividing the tile), tiles without (bs 96, 160, 320), and blocks above
+    65536 whose micro table is built one level per table step ("huge")."""
     from rtxrmq_gb300.batch import RMQBatch
     starts, lengths, qstarts, qcounts, A, Q = small_ragged(seed, ties, align)
     bucket_bs = {"default": None, "small": [64] * 32, "large": [65536] * 32,
+                 "huge": [1 << 18] * 32,
                  "mixed": [64, 96, 128, 160, 320, 1024, 2048, 4096] * 4}[cfg]
     ev, ei = expected(oracle_lib, starts, lengths, qstarts, qcounts, A, Q)
     own = owned_mask(qstarts, qcounts, len(Q))

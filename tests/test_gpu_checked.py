@@ -179,6 +179,8 @@ for seed in range(24):
     # the same batch as a light plan (block sizes made multiples of 32, >= 64),
     # and as int32 range maximum over the same values scaled to integers
     lbs = [0 if x <= 0 else max(64, x // 32 * 32) for x in bucket_bs]
+    if seed % 4 == 3:
+        lbs = [1 << 18] * 32  # micro table one level per table step
     with RMQBatch(starts, lengths, qstarts, qcounts, lbs, light=True) as b:
         dVr, dQr = torch.from_numpy(V).to(dev), torch.from_numpy(Qr).to(dev)
         v, i = b.run(dVr, dQr)
