@@ -364,9 +364,14 @@ int rmq_batch_create_ex(int32_t narrays, const int64_t *h_starts, const int64_t 
             // item per micro level. B: block minima from the micro-block
             // minima unless the tiles wrote them, then block level k.
             const uint32_t pb = a.bs / kMicro;
-            if ((1u << (a.mlevels - 1)) - 1u <= kMicroHaloMax) {
-                a.light_flags = kLightTiled | (kMicroTile % pb == 0 ? kLightTileBmin : 0u);
-                for (uint32_t t = 0; t * kMicroTile < a.nmicro; ++t) build.push_back(make_uint2(i, t));
+            const uint32_t halo = (1u << (a.mlevels - 1)) - 1u;
+            const uint32_t tile = halo + kMicroTile <= kTileEntries        ? kMicroTile
+                                  : halo + kMicroTileSmall <= kTileEntries ? kMicroTileSmall
+                                                                           : 0u;
+            if (tile) {
+                a.light_flags = kLightTiled | (tile % pb == 0 ? kLightTileBmin : 0u) |
+                                (tile == kMicroTileSmall ? kLightSmallTile : 0u);
+                for (uint32_t t = 0; t * tile < a.nmicro; ++t) build.push_back(make_uint2(i, t));
             } else {
                 for (uint32_t c = 0; c * kLightChunk < a.nmicro; ++c) build.push_back(make_uint2(i, c));
                 for (uint32_t k = 1; k < a.mlevels && (1u << k) <= a.nmicro; ++k)

@@ -52,16 +52,19 @@ enum : uint32_t {
     kItemMicroLevel = 2,   // micro-table level k from level k - 1
 };
 // Light tiles (phase A items of a light array whose micro table is shallow
-// enough): kMicroTile micro-blocks whose minima, every micro-table level and
-// the minima of the blocks inside come from one read of the tile's values
-// plus a halo of 2^(mlevels - 1) - 1 micro-blocks (at most kMicroHaloMax:
-// blocks up to 65536 elements). Other light arrays take chunks in phase A
-// and one table item per level.
+// enough): kMicroTile (or kMicroTileSmall) micro-blocks whose minima, every
+// micro-table level and the minima of the blocks inside come from one read
+// of the tile's values plus a halo of 2^(mlevels - 1) - 1 micro-blocks. The
+// levels are built in two shared-memory buffers of kTileEntries minima each,
+// so tile + halo <= kTileEntries: tiles of 2048 up to bs 32768, of 1024 at
+// bs 65536. Other light arrays take chunks in phase A and one table item
+// per level.
 constexpr uint32_t kMicroTile = 2048;
-constexpr uint32_t kMicroHaloMax = 2047;
+constexpr uint32_t kMicroTileSmall = 1024;
 // BatchArray::light_flags
 constexpr uint32_t kLightTiled = 1;       // phase A items are tiles
-constexpr uint32_t kLightTileBmin = 2;    // tiles also write the block minima (bs / 32 divides kMicroTile)
+constexpr uint32_t kLightTileBmin = 2;    // tiles also write the block minima (bs / 32 divides the tile)
+constexpr uint32_t kLightSmallTile = 4;   // tiles of kMicroTileSmall
 
 struct BatchArray {
     int64_t off;    // first value in the buffer
@@ -102,8 +105,10 @@ constexpr size_t kLightQueueBytes = sizeof(MissQueue) * (kBatchThreads / 32);
 constexpr size_t kLightSmemBytes =
     kLightQueueBytes + sizeof(uint4) * kLineChunks * static_cast<size_t>(kBatchThreads);
 static_assert(kLightQueueBytes % 16 == 0, "line slots start 16-byte aligned");
-static_assert((kMicroTile + kMicroHaloMax) * (sizeof(Entry) + sizeof(uint16_t)) <= kLightSmemBytes,
-              "a light tile fits the light CTA's shared memory");
+// minima per buffer of a light tile (two buffers)
+constexpr uint32_t kTileEntries = static_cast<uint32_t>(kLightSmemBytes / (2 * sizeof(Entry)));
+static_assert(kTileEntries >= kMicroTile + 1023 && kTileEntries >= kMicroTileSmall + 2047,
+              "tiles of 2048 up to bs 32768 and of 1024 at bs 65536 fit");
 
 // Light kernels (batch_light.cu): the instantiation for (aligned, key mode),
 // its dynamic shared memory and CTAs per SM (the dynamic-memory limit set).
@@ -226,62 +231,49 @@ __device__ __forceinline__ void light_micro_level_w(const BatchParams &P, const 
 }
 
 // Every level 1 .. mlevels - 1 of the micro table at positions [t0, t0 +
-// count) from the minima key[0 .. e) of micro-blocks [t0, t0 + e) in shared
-// memory (best[i] = i on entry). Each level keeps, per position, the
-// tile-local index of its window's best micro-block (the level below's two
-// halves compared); positions whose window leaves the loaded range are
-// dropped level by level. Two barriers per level separate the reads of the
-// level below from the overwrite.
+// count) from the minima src[0 .. e) of micro-blocks [t0, t0 + e) in shared
+// memory. Level k holds the best minimum of every window of 2^k micro-blocks
+// whose window lies in the loaded range (the better of the level below's two
+// halves), written to the other buffer; the offset stored is that minimum's
+// micro-block (its element index / 32) minus the window's first. One barrier
+// per level.
 template <class O>
 __device__ __forceinline__ void micro_tile_levels(const BatchParams &P, const BatchArray &a,
                                                   uint32_t t0, uint32_t count, uint32_t e,
-                                                  const Entry *key, uint16_t *best) {
-    constexpr int kPer = (kMicroTile + kMicroHaloMax + kBatchThreads - 1) / kBatchThreads;
+                                                  Entry *src, Entry *dst) {
     O *off = reinterpret_cast<O *>(P.ws + a.moff);
     for (uint32_t k = 1; k < a.mlevels && (1u << k) <= e; ++k) {
         const uint32_t half = 1u << (k - 1);
         const uint32_t valid = e - (1u << k) + 1;  // windows inside the loaded range
-        uint16_t nb[kPer];
-#pragma unroll
-        for (int r = 0; r < kPer; ++r) {
-            const uint32_t i = threadIdx.x + r * kBatchThreads;
-            nb[r] = 0;
-            if (i < valid) {
-                const uint16_t x = best[i], y = best[i + half];
-                nb[r] = key[y] < key[x] ? y : x;
-            }
-        }
-        __syncthreads();
         O *__restrict__ row = off + static_cast<size_t>(k - 1) * a.nmicro + t0;
-#pragma unroll
-        for (int r = 0; r < kPer; ++r) {
-            const uint32_t i = threadIdx.x + r * kBatchThreads;
-            if (i < valid) {
-                best[i] = nb[r];
-                if (i < count) row[i] = static_cast<O>(nb[r] - i);
-            }
+        for (uint32_t i = threadIdx.x; i < valid; i += kBatchThreads) {
+            const Entry m = better(src[i], src[i + half]);
+            dst[i] = m;
+            if (i < count) row[i] = static_cast<O>((entry_idx(m) >> 5) - (t0 + i));
         }
         __syncthreads();
+        Entry *t = src;
+        src = dst;
+        dst = t;
     }
 }
 
 // Light phase A, one tile (kLightTiled arrays): the minima of micro-blocks
-// [t0, t0 + count + halo) from the values into shared memory (16 per warp
-// per step, as light_chunk), the tile's own minima to the micro-block minima
-// table, the minima of the blocks inside the tile (kLightTileBmin), and every
-// micro-table level at [t0, t0 + count). The halo's minima are computed
-// again by the next tile.
+// [t0, t0 + count + halo) from the values into shared memory (8 rows of 512
+// bytes per warp step, all loads in flight), the tile's own minima to the
+// micro-block minima table, the minima of the blocks inside the tile
+// (kLightTileBmin), and every micro-table level at [t0, t0 + count). The
+// halo's minima are computed again by the next tile.
 template <bool ALIGNED, uint32_t MODE, class O>
 __device__ __forceinline__ void light_tile(const BatchParams &P, const BatchArray &a, uint32_t t,
                                            unsigned char *smem) {
-    constexpr uint32_t kMaxE = kMicroTile + kMicroHaloMax;
     Entry *key = reinterpret_cast<Entry *>(smem);
-    uint16_t *best = reinterpret_cast<uint16_t *>(key + kMaxE);
-    const uint32_t t0 = t * kMicroTile;
-    const uint32_t count = min(kMicroTile, a.nmicro - t0);
+    const uint32_t tile = (a.light_flags & kLightSmallTile) ? kMicroTileSmall : kMicroTile;
+    const uint32_t t0 = t * tile;
+    const uint32_t count = min(tile, a.nmicro - t0);
     const uint32_t halo = (1u << (a.mlevels - 1)) - 1u;
     const uint32_t jend = min(t0 + count + halo, a.nmicro);
-    const uint32_t e = jend - t0;  // minima held in shared memory
+    const uint32_t e = jend - t0;  // minima held in shared memory (<= kTileEntries)
     const float *A = P.A + a.off;
     const bool vec = ALIGNED && a.off % 4 == 0;
     // 8 rows (32 micro-blocks, 4 KB) per warp step: 96 KB of loads in flight per SM
@@ -295,10 +287,7 @@ __device__ __forceinline__ void light_tile(const BatchParams &P, const BatchArra
     }
     __syncthreads();
     Entry *mst = P.ws + a.mst;
-    for (uint32_t i = threadIdx.x; i < e; i += kBatchThreads) {
-        if (i < count) mst[t0 + i] = key[i];
-        best[i] = static_cast<uint16_t>(i);
-    }
+    for (uint32_t i = threadIdx.x; i < count; i += kBatchThreads) mst[t0 + i] = key[i];
     if (a.light_flags & kLightTileBmin) {
         // blocks [t0 / pb, (t0 + count - 1) / pb], all inside the tile
         const uint32_t pb = a.bs / kMicroElems;
@@ -323,8 +312,10 @@ __device__ __forceinline__ void light_tile(const BatchParams &P, const BatchArra
             }
         }
     }
-    __syncthreads();
-    micro_tile_levels<O>(P, a, t0, count, e, key, best);
+    // the levels write only the second buffer first; the block minima and
+    // the table copy above read the first
+    micro_tile_levels<O>(P, a, t0, count, e, key, key + kTileEntries);
+    __syncthreads();  // the next tile overwrites both buffers
 }
 
 // Phase B: table steps 1 .. maxlev - 1, a grid barrier after each.
