@@ -417,14 +417,37 @@ __device__ __forceinline__ Entry line_min_async(const V1View &v, uint32_t lo, ui
     for (int c = 0; c < nc; ++c) {
         const uint4 f = slot[c];
         const uint32_t w[4] = {f.x, f.y, f.z, f.w};
+        const int32_t c0 = l0 + 4 * c;  // local index of w[0]
+        if constexpr (MODE == kFloatMin || MODE == kFloatMax) {
+            // the chunk's IEEE minimum (maximum) over its values in [lo, hi]
+            // (others as NaN, which it skips), the first value equal to it,
+            // and one key from that value's bits
+            float x[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int32_t li = l0 + 4 * c + k;
-            const uint32_t kk = key_of(w[k], MODE);
-            if (static_cast<uint32_t>(li - static_cast<int32_t>(lo)) <= hi - lo && kk < km) {
+            for (int k = 0; k < 4; ++k)
+                x[k] = __uint_as_float(
+                    static_cast<uint32_t>(c0 + k - static_cast<int32_t>(lo)) <= hi - lo
+                        ? w[k] : 0x7fc00000u);
+            const float m = MODE == kFloatMin ? fminf(fminf(x[0], x[1]), fminf(x[2], x[3]))
+                                              : fmaxf(fmaxf(x[0], x[1]), fmaxf(x[2], x[3]));
+            const uint32_t p = x[0] == m ? 0u : x[1] == m ? 1u : x[2] == m ? 2u : x[3] == m ? 3u : 0u;
+            const uint32_t wb = __float_as_uint(p == 0u ? x[0] : p == 1u ? x[1] : p == 2u ? x[2] : x[3]);
+            const uint32_t kk = key_of(wb, MODE);
+            if (kk < km) {
                 km = kk;
-                pos = static_cast<uint32_t>(li);
-                nz = negzero_of(w[k], MODE);
+                pos = static_cast<uint32_t>(c0) + p;
+                nz = negzero_of(wb, MODE);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int32_t li = c0 + k;
+                const uint32_t kk = key_of(w[k], MODE);
+                if (static_cast<uint32_t>(li - static_cast<int32_t>(lo)) <= hi - lo && kk < km) {
+                    km = kk;
+                    pos = static_cast<uint32_t>(li);
+                    nz = negzero_of(w[k], MODE);
+                }
             }
         }
     }
