@@ -711,6 +711,12 @@ def bench_batched(args, dev, stream, barrier):
                          for k, v in enumerate(lcfg) if v[0]},
         # one read of the values, 8 B per 32 elements of micro-block minima
         "build_alg_bytes": int(w.lengths.sum()) * 4 + int(w.lengths.sum()) // 32 * 8}
+    # the faster plan of the two (same answers, checked above)
+    best_light = lgms < gms and lmatch
+    res["best"] = {"index": "light" if best_light else "full",
+                   "batched_graph_rmq_s": job_rate(q, nr, lgms if best_light else gms),
+                   "batched_graph_ms": lgms if best_light else gms,
+                   "speedup_vs_per_array": pms / (lgms if best_light else gms)}
     res.update({"batched_graph_rmq_s": job_rate(q, nr, gms), "batched_graph_ms": gms,
                 "batched_rmq_s": job_rate(q, nr, ms), "batched_ms": ms,
                 "per_array_rmq_s": job_rate(q, nr, pms), "per_array_ms": pms,
