@@ -6,12 +6,14 @@
 // Persistent kernel, three phases separated by grid-wide barriers of a
 // cooperative launch (all CTAs are co-resident, guaranteed by the launch):
 //   A  build items. Full: (array, unit) prefix/suffix minima + block minima,
-//      the plain builder's CTA body (build_impl.cuh). Light: (array, chunk)
-//      minima of 128 micro-blocks, 16 per warp;
+//      the plain builder's CTA body (build_impl.cuh). Light: (array, tile)
+//      micro-block minima, every micro-table level and the block minima of
+//      a tile, from one read of its values (light_tile); for block sizes
+//      above 65536, (array, chunk) micro-block minima only;
 //   B  table items (array, kind | level, first entry, count), one step per
-//      barrier. Full: step k computes block-table level k. Light: step k
-//      computes block-table level k - 1 (level 0, the block minima, from
-//      the micro-block minima) and micro-table level k;
+//      barrier: block-table level k at step k (at step k + 1 when step 1
+//      computes the block minima from the micro-block minima), and for
+//      untiled light arrays micro-table level k at step k;
 //   C  query items (array, first query, count), query_impl.cuh's queued
 //      form (light: misses settle from value lines, no entries).
 // Work lists are built on the host once per plan, so a run allocates nothing
