@@ -356,6 +356,36 @@ def test_batch_argument_types(native):
         B._queries(torch.zeros((4, 2), dtype=torch.int64))
     with pytest.raises(TypeError):
         B._queries(torch.zeros((4, 3), dtype=torch.int32))
+    # an int32 plan takes int32 values only (on the CPU a value tensor of the
+    # right type passes the type check and is refused as not on the device)
+    with pytest.raises(ValueError):
+        B._vals(torch.zeros(4, dtype=torch.int32), int32=True)
+    with pytest.raises(TypeError):
+        B._vals(torch.zeros(4, dtype=torch.float32), int32=True)
+    with pytest.raises(TypeError):
+        B._vals(torch.zeros(4, dtype=torch.int32))
+
+
+def test_batch_plan_flags(native):
+    """RMQBatch(op, dtype, light) maps to rmq_batch_create_ex's flags
+    (include/rmq.h's RMQ_BUILD_* bits), from strings or torch dtypes."""
+    import torch
+
+    from rtxrmq_gb300 import batch as B
+    from rtxrmq_gb300._native import RMQ_BUILD_INT32, RMQ_BUILD_LIGHT, RMQ_BUILD_MAX
+    assert B.plan_flags() == 0
+    assert B.plan_flags("max") == RMQ_BUILD_MAX
+    assert B.plan_flags(dtype="int32") == B.plan_flags(dtype=torch.int32) == RMQ_BUILD_INT32
+    assert B.plan_flags("max", torch.int32, True) == RMQ_BUILD_MAX | RMQ_BUILD_INT32 | RMQ_BUILD_LIGHT
+    assert B.plan_flags(dtype=torch.float32, light=True) == RMQ_BUILD_LIGHT
+    header = (Path(__file__).resolve().parent.parent / "include" / "rmq.h").read_text()
+    for name, val in (("RMQ_BUILD_MAX", RMQ_BUILD_MAX), ("RMQ_BUILD_INT32", RMQ_BUILD_INT32),
+                      ("RMQ_BUILD_LIGHT", RMQ_BUILD_LIGHT)):
+        assert re.search(rf"#define {name}\s+{val}u", header), name
+    with pytest.raises(ValueError):
+        B.plan_flags("median")
+    with pytest.raises(TypeError):
+        B.plan_flags(dtype="float64")
 
 
 def test_random_parity_cases_are_valid(native):
