@@ -38,6 +38,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "lane_min.cuh"
 
 namespace rmq {
 
@@ -743,7 +744,7 @@ constexpr uint32_t kMicroPerWarp = 16;  // micro-blocks a warp reduces per step
 // on the 8 lanes of group `grp` (this lane's first element at e = base +
 // 4 sub). Composites order by (key, index), so the 32-bit keys are reduced
 // first: each lane keeps its smallest key and the first position holding
-// it, the group takes the minimum key, and the leftmost lane holding that
+// it (lane_best4), the group takes the minimum key, and the leftmost lane holding that
 // key owns the leftmost best element; its position and -0.0 flag come over
 // in one shuffle. Elements at or past n take the largest key; they lie to
 // the right of every valid element, so a tie never selects one.
@@ -751,34 +752,7 @@ template <uint32_t MODE, bool FULL>
 __device__ __forceinline__ Entry micro_row_min(const uint32_t (&b)[4], uint32_t e, uint32_t n,
                                                uint32_t grp, uint32_t sub) {
     uint32_t km, info;  // the lane's best key; its position | (-0.0 flag << 2)
-    if constexpr (MODE == kFloatMin || MODE == kFloatMax) {
-        // The lane's best value by IEEE minNum / maxNum, which skips NaN (last
-        // in the key order) unless all four are NaN; the first element equal
-        // to it (+0 == -0, so the leftmost zero) is the leftmost best, and its
-        // bits give the key and the -0.0 flag. Elements past n become NaN and
-        // lie to the right of every valid one. All NaN: element 0.
-        float f[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            f[k] = __uint_as_float((FULL || e + k < n) ? b[k] : 0x7fc00000u);
-        const float m = MODE == kFloatMin ? fminf(fminf(f[0], f[1]), fminf(f[2], f[3]))
-                                          : fmaxf(fmaxf(f[0], f[1]), fmaxf(f[2], f[3]));
-        const uint32_t pos = f[0] == m ? 0u : f[1] == m ? 1u : f[2] == m ? 2u : f[3] == m ? 3u : 0u;
-        const uint32_t wb = __float_as_uint(pos == 0u ? f[0] : pos == 1u ? f[1] : pos == 2u ? f[2] : f[3]);
-        km = key_of(wb, MODE);
-        info = pos | (negzero_of(wb, MODE) << 2);
-    } else {
-        km = (FULL || e < n) ? key_of(b[0], MODE) : 0xffffffffu;
-        info = negzero_of(b[0], MODE) << 2;
-#pragma unroll
-        for (int k = 1; k < 4; ++k) {
-            const uint32_t kk = (FULL || e + k < n) ? key_of(b[k], MODE) : 0xffffffffu;
-            if (kk < km) {
-                km = kk;
-                info = static_cast<uint32_t>(k) | (negzero_of(b[k], MODE) << 2);
-            }
-        }
-    }
+    lane_best4<MODE>(b, FULL ? 4u : (e < n ? min(4u, n - e) : 0u), km, info);
     uint32_t gk = km;
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) gk = min(gk, __shfl_xor_sync(0xffffffffu, gk, o, 8));

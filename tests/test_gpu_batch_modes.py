@@ -200,3 +200,35 @@ def test_batch_light_autotune(cuda, native, oracle_lib, tmp_path):
         torch.cuda.synchronize()
     np.testing.assert_array_equal(i.cpu().numpy()[own], ei[own])
     np.testing.assert_array_equal(bits(v.cpu().numpy()[own]), bits(ev[own]))
+
+
+@pytest.mark.parametrize("light", [False, True])
+@pytest.mark.parametrize("op", ["min", "max"])
+def test_batch_nan_and_signed_zero_order(cuda, native, op, light):
+    """Batched plans over arrays holding quiet and signaling NaNs and +-0:
+    the same order as the plain index (NaN last, canonical NaN returned,
+    -0 == +0 leftmost), every path."""
+    from test_gpu_light import expect_nan_case, nan_case
+
+    from rtxrmq_gb300.batch import RMQBatch
+    A, Qall = nan_case(21 + light, 12011)
+    # three arrays over the buffer at odd offsets, each with its own queries
+    starts = np.array([0, 4001, 8003], np.int64)
+    lengths = np.array([4000, 4001, 4007], np.int64)
+    qs, ev_all, ei_all = [], [], []
+    for s, n in zip(starts, lengths):
+        Q = Qall[(Qall[:, 1] < n)][:6000]
+        ei, ev = expect_nan_case(A[s:s + n], Q, op)
+        qs.append(Q)
+        ei_all.append(ei)
+        ev_all.append(ev)
+    qcounts = np.array([len(q) for q in qs], np.int64)
+    qstarts = np.concatenate([[0], np.cumsum(qcounts)[:-1]]).astype(np.int64)
+    Q = np.concatenate(qs)
+    ei, ev = np.concatenate(ei_all), np.concatenate(ev_all)
+    with RMQBatch(starts, lengths, qstarts, qcounts, [64, 256, 1024, 4096] * 8, op=op,
+                  light=light) as b:
+        outs = run_all(cuda, b, A, Q)
+    for v, i in outs:
+        np.testing.assert_array_equal(i, ei)
+        np.testing.assert_array_equal(v.view(np.uint32), ev)

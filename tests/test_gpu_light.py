@@ -156,3 +156,70 @@ def test_light_query_stats(cuda, native, bs, lr):
     assert settled == q
     if st["second_probe"] + st["full"]:
         assert st["scan_sectors"] > st["micro_scan"]
+
+
+def key_order(bits, op):
+    """The engine's order of float32 values (as uint32 bits): -0 == +0, NaN
+    (quiet or signaling, either sign) after every number; for op "max" the
+    reverse of the numbers, NaN still last."""
+    b = bits.astype(np.uint32)
+    a = b & np.uint32(0x7fffffff)
+    k = np.where(b >> 31 == 1, ~b, b | np.uint32(0x80000000)).astype(np.uint32)
+    k[a == 0] = np.uint32(0x80000000)
+    nan = a > np.uint32(0x7f800000)
+    if op == "max":
+        k = ~k
+    k[nan] = np.uint32(0xffffffff)
+    return k
+
+
+def nan_case(seed, n):
+    """float32 values with quiet and signaling NaNs of both signs, +-0 and
+    +-inf among normal values, and queries of every length class."""
+    import rtxrmq_gb300 as R
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal(n).astype(np.float32)
+    bits = A.view(np.uint32)
+    for pattern, cnt in ((0x7fc00000, n // 40), (0xffc00000, n // 40), (0x7f800001, n // 40),
+                         (0xffbfffff, n // 40), (0x00000000, n // 30), (0x80000000, n // 30),
+                         (0x7f800000, 20), (0xff800000, 20)):
+        bits[rng.integers(0, n, cnt)] = pattern
+    # runs of NaN only, so that some queries see nothing else
+    for s in rng.integers(0, n - 100, 10):
+        bits[s:s + int(rng.integers(1, 90))] = rng.choice([0x7fc00000, 0xffbfffff, 0x7f800001])
+    Q = np.concatenate([R.gen_queries(4000, n, L, seed + L) for L in (1, 2, 5, 33, 300, 3000)])
+    return A, Q
+
+
+def expect_nan_case(A, Q, op):
+    k = key_order(A.view(np.uint32), op)
+    ei = np.array([l + int(np.argmin(k[l:r + 1])) for l, r in Q], dtype=np.int32)
+    ev = np.where(k[ei] == np.uint32(0xffffffff), np.uint32(0x7fc00000), A.view(np.uint32)[ei])
+    return ei, ev
+
+
+@pytest.mark.parametrize("op", ["min", "max"])
+@pytest.mark.parametrize("light", [False, True])
+def test_nan_and_signed_zero_order(cuda, native, op, light):
+    """NaNs (quiet and signaling, both signs) order after every number and
+    come back as the canonical quiet NaN; +-0 are equal (leftmost wins, its
+    own sign returned). Full and light index, both float modes, block sizes
+    across the micro-block and block paths; the light index's micro-block
+    minima take each lane's IEEE minimum, which must skip every NaN."""
+    n = 6007
+    A, Q = nan_case(11 + light, n)
+    ei, ev = expect_nan_case(A, Q, op)
+    for bs in (64, 256, 2048):
+        v, i, _ = run_light(cuda, A, Q, bs, op=op) if light else run_full(cuda, A, Q, bs, op)
+        np.testing.assert_array_equal(i, ei)
+        np.testing.assert_array_equal(v.view(np.uint32), ev)
+
+
+def run_full(cuda, A, Q, bs, op):
+    import torch
+
+    import rtxrmq_gb300 as R
+    with R.RMQIndex(torch.from_numpy(A).to(cuda), bs, op=op) as ix:
+        v, i = ix.query(torch.from_numpy(np.ascontiguousarray(Q, dtype=np.int32)).to(cuda))
+        torch.cuda.synchronize()
+        return v.cpu().numpy(), i.cpu().numpy(), None

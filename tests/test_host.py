@@ -164,6 +164,73 @@ def test_device_helpers_on_host(tmp_path, native):
     assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr
 
 
+LANE_TEST = r"""
+#include <cstdio>
+#include <vector>
+#include "lane_min.cuh"
+using namespace rmq;
+static unsigned long long rng = 0x9E3779B97F4A7C15ull;
+static unsigned next() { rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17; return (unsigned)rng; }
+// definition: among b[0 .. nvalid), the smallest key, leftmost among equal
+// keys; no valid value: the largest key at position 0
+template <uint32_t MODE> static bool check(const uint32_t (&b)[4], uint32_t nvalid) {
+  uint32_t ek = 0xffffffffu, ep = 0u, en = 0u;
+  for (uint32_t k = 0; k < nvalid; ++k) {
+    const uint32_t kk = key_of(b[k], MODE);
+    if (k == 0 || kk < ek) { ek = kk; ep = k; en = negzero_of(b[k], MODE); }
+  }
+  uint32_t key, info;
+  lane_best4<MODE>(b, nvalid, key, info);
+  const uint32_t want = ep | (en << 2);
+  if (key != ek || (nvalid > 0 && info != want) || (nvalid == 0 && (info & 3u) != 0u)) {
+    std::printf("mode %u nvalid %u: %08x %08x %08x %08x -> key %08x info %u, want %08x %u\n", MODE,
+                nvalid, b[0], b[1], b[2], b[3], key, info, ek, want);
+    return false;
+  }
+  return true;
+}
+int main() {
+  // special values: +-0, +-inf, NaNs of both signs and payloads, subnormals,
+  // the extremes, small integers (ties), and random bits
+  std::vector<unsigned> pool = {0u, 0x80000000u, 0x7f800000u, 0xff800000u, 0x7fc00000u,
+      0xffc00000u, 0x7f800001u, 0xffbfffffu, 1u, 0x80000001u, 0x007fffffu, 0x807fffffu,
+      0x3f800000u, 0xbf800000u, 0x7f7fffffu, 0xff7fffffu, 0x40000000u, 0xc0000000u,
+      0x80000000u, 0x00000000u, 0x7fffffffu, 0xffffffffu};
+  for (int i = 0; i < 24; ++i) pool.push_back(next());
+  long n = 0;
+  for (int it = 0; it < 120000; ++it) {
+    uint32_t b[4];
+    for (int k = 0; k < 4; ++k) b[k] = (next() & 3) ? pool[next() % pool.size()] : next();
+    for (uint32_t nv = 0; nv <= 4; ++nv) {
+      if (!check<kFloatMin>(b, nv) || !check<kFloatMax>(b, nv) || !check<kIntMin>(b, nv) ||
+          !check<kIntMax>(b, nv)) return 1;
+      ++n;
+    }
+  }
+  std::printf("ok %ld\n", n);
+  return 0;
+}
+"""
+
+
+def test_lane_minimum_matches_key_order(tmp_path, native):
+    """lane_best4 (the per-lane step of the light index's micro-block minima),
+    compiled for the host: for four values with any number valid, in every
+    key mode, the key and position of the smallest key, leftmost among equal
+    keys. Covers +-0 ties, NaNs of either sign, subnormals and infinities,
+    where the float modes' IEEE minimum / maximum path must agree with the
+    key order."""
+    src = tmp_path / "lane.cpp"
+    src.write_text(LANE_TEST)
+    exe = tmp_path / "lane"
+    r = subprocess.run(["g++", "-O2", "-std=c++17", f"-I{ROOT / 'rtxrmq_gb300' / 'csrc'}",
+                        "-I/usr/local/cuda/include", str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
+
+
 CLI = ROOT / "rtxrmq_gb300" / "_lib" / "rtxrmq"
 
 
